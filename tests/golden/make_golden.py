@@ -1,0 +1,254 @@
+"""Generate the golden fixtures in this folder from the reference's own code.
+
+Run from the repository root in a container that has the reference checkout:
+
+    python tests/golden/make_golden.py
+
+The reference's hot-path modules are loaded from their source files through
+``ref_shim`` (numpy stand-ins for jax/numba; see its docstring for what that does
+and does not reproduce) and run on small seeded inputs.  Inputs and outputs are
+written to ``tests/golden/*.npz``; the tests only read those files, so neither the
+reference nor this script is needed to run them.
+"""
+
+from __future__ import annotations
+
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(HERE.parent.parent))
+
+import ref_shim  # noqa: E402
+
+from dolphin_gb300.simulate import StackConfig, make_stack  # noqa: E402
+
+R = ref_shim.load_reference()
+HW = R.types.HalfWindow
+ST = R.types.Strides
+
+
+def _save(name, **arrays):
+    path = HERE / f"{name}.npz"
+    np.savez_compressed(path, **arrays)
+    print(f"wrote {path.name}: {path.stat().st_size / 1024:.0f} KiB")
+
+
+def make_ps():
+    rng = np.random.default_rng(101)
+    n, rows, cols = 12, 17, 23
+    mag = rng.lognormal(0.0, 0.5, size=(n, rows, cols)).astype(np.float32)
+    # low-dispersion pixels (PS-like), a constant pixel (dispersion 0), NaN patterns
+    mag[:, 2, 3] = (10 * (1 + 0.01 * rng.normal(size=n))).astype(np.float32)
+    mag[:, 5, 5] = (8 * (1 + 0.2 * rng.normal(size=n))).astype(np.float32)
+    mag[:, 7, 9] = np.float32(4.0)
+    mag[0, 1, 1] = np.nan
+    mag[:3, 4, 4] = np.nan
+    mag[:, 6, 6] = np.nan
+    mag[:, 10:12, 14:18] = (5 * (1 + 0.05 * rng.normal(size=(n, 2, 4)))).astype(np.float32)
+    cases = [(0.25, None), (0.4, n), (0.35, 9), (1e5, None), (0.0, None)]
+    out = {"mag": mag, "thr": np.array([c[0] for c in cases]),
+           "min_count": np.array([-1 if c[1] is None else c[1] for c in cases])}
+    for k, (thr, mc) in enumerate(cases):
+        mean, disp, ps = R.ps.calc_ps_block(mag.copy(), thr, mc)
+        out[f"mean_{k}"], out[f"disp_{k}"], out[f"ps_{k}"] = mean, disp, ps
+    _save("ps_block", **out)
+
+
+def _amp_field(seed, n, rows, cols):
+    rng = np.random.default_rng(seed)
+    amp = rng.rayleigh(scale=10.0, size=(n, rows, cols)).astype(np.float32)
+    amp[:, : rows // 3, :] *= np.float32(3.0)  # a bright region with a sharp edge
+    amp[:, :, cols - 4 :] *= np.float32(0.4)
+    return amp
+
+
+def make_glrt():
+    out = {}
+    cases = [
+        # (seed, n, rows, cols, hw, strides, nslc, alpha)
+        (201, 30, 24, 30, (3, 5), (1, 1), 30, 0.001),
+        (202, 20, 22, 26, (5, 5), (2, 2), 20, 0.005),
+        (203, 12, 19, 27, (2, 4), (2, 3), 12, 0.05),
+        (204, 30, 16, 40, (5, 11), (1, 1), 30, 0.001),
+    ]
+    for k, (seed, n, rows, cols, hw, st, nslc, alpha) in enumerate(cases):
+        amp = _amp_field(seed, n, rows, cols)
+        mean = np.mean(amp, axis=0)
+        var = np.var(amp, axis=0)
+        mean[:3, :4] = 0  # nodata convention: mean 0 gives no SHPs
+        nb = np.asarray(
+            R.shp.estimate_neighbors(
+                mean=mean, var=var, halfwin_rowcol=hw, strides=ST(*st), nslc=nslc,
+                alpha=alpha, method="glrt",
+            )
+        )
+        out[f"mean_{k}"], out[f"var_{k}"], out[f"nb_{k}"] = mean, var, nb
+        out[f"params_{k}"] = np.array([*hw, *st, nslc, alpha], dtype=np.float64)
+    _save("glrt", ncases=np.array(len(cases)), **out)
+
+
+def make_ks():
+    out = {}
+    cases = [
+        (301, 16, 14, 18, (2, 3), (1, 1), 0.05),
+        (302, 11, 13, 15, (3, 3), (2, 2), 0.01),
+        (303, 30, 11, 11, (5, 5), (1, 1), 1e-6),
+    ]
+    for k, (seed, n, rows, cols, hw, st, alpha) in enumerate(cases):
+        amp = _amp_field(seed, n, rows, cols)
+        if k == 0:
+            amp[:, 6, 8] = amp[:, 6, 7]  # exact ties between two pixels
+            amp[3, 5, 5] = np.nan
+        nb = np.asarray(
+            R.shp.estimate_neighbors(
+                amp_stack=amp, halfwin_rowcol=hw, strides=ST(*st), nslc=n, alpha=alpha,
+                method="ks",
+            )
+        )
+        out[f"amp_{k}"], out[f"nb_{k}"] = amp, nb
+        out[f"params_{k}"] = np.array([*hw, *st, alpha], dtype=np.float64)
+    crit = []
+    for n in (5, 8, 10, 15, 20, 30, 45, 64):
+        for alpha in (1e-6, 0.001, 0.01, 0.05, 0.5):
+            crit.append((n, alpha, R.ks._get_ecdf_critical_distance(n, alpha)))
+    out["crit"] = np.array(crit, dtype=np.float64)
+    # the reference's own doctest vectors for the ECDF distance (shp/_ks.py:180-194)
+    x1 = np.array([1, 2, 3, 4, 5], dtype=np.float64)
+    pairs = [x1, np.array([2, 3, 4, 5, 6.0]), np.array([6, 7, 8, 9, 10.0])]
+    out["cdf_x"] = np.stack(pairs)
+    out["cdf_d"] = np.array([R.ks._get_max_cdf_dist(x1, p) for p in pairs])
+    _save("ks", ncases=np.array(len(cases)), **out)
+
+
+def make_covariance():
+    out = {}
+    z = make_stack(StackConfig(nslc=8, rows=14, cols=17, seed=401, ps_frac=0.0))
+    z[2, 3, 4] = np.nan
+    z[:, 9, 10] = np.nan
+    amp = np.abs(z)
+    nb = np.asarray(
+        R.shp.estimate_neighbors(
+            mean=np.nanmean(amp, 0), var=np.nanvar(amp, 0), halfwin_rowcol=(3, 4),
+            strides=ST(1, 1), nslc=8, alpha=0.05, method="glrt",
+        )
+    )
+    out["slc"] = z
+    out["nb"] = nb
+    out["C_rect"] = np.asarray(R.covariance.estimate_stack_covariance(z, HW(3, 4), ST(1, 1)))
+    out["C_nb"] = np.asarray(
+        R.covariance.estimate_stack_covariance(z, HW(3, 4), ST(1, 1), neighbor_arrays=nb)
+    )
+    out["C_strided"] = np.asarray(R.covariance.estimate_stack_covariance(z, HW(3, 4), ST(2, 3)))
+    _save("covariance", **out)
+
+
+def _pl_case(idx, z, hw, strides, **kw):
+    t0 = time.time()
+    res = R.core.run_phase_linking(z.copy(), HW(*hw), ST(*strides), **kw)
+    print(f"  case {idx}: {time.time() - t0:.1f}s")
+    out = {f"{idx}_{k}": np.asarray(v) for k, v in res._asdict().items()}
+    return out
+
+
+def make_phase_link():
+    cfg = StackConfig(nslc=10, rows=18, cols=22, seed=501, ps_frac=0.04)
+    z, ps_truth, _ = make_stack(cfg, return_truth=True)
+    amp = np.abs(z)
+    mean, disp, ps = R.ps.calc_ps_block(amp.copy(), 0.25, cfg.nslc)
+    var = (disp * mean) ** 2
+    nodata = np.zeros(z.shape[1:], bool)
+    nodata[0, :3] = True
+    zn = z.copy()
+    zn[4, 15:, 19:] = np.nan  # a corner that is NaN in one SLC -> nodata
+    nb11 = np.asarray(
+        R.shp.estimate_neighbors(mean=mean, var=var, halfwin_rowcol=(3, 4), strides=ST(1, 1),
+                                 nslc=cfg.nslc, alpha=0.001, method="glrt"))
+    nb23 = np.asarray(
+        R.shp.estimate_neighbors(mean=mean, var=var, halfwin_rowcol=(3, 4), strides=ST(2, 3),
+                                 nslc=cfg.nslc, alpha=0.001, method="glrt"))
+    out = {"slc": z, "slc_nan": zn, "ps": ps, "nodata": nodata, "mean": mean, "nb11": nb11,
+           "nb23": nb23}
+    specs = {
+        0: dict(z="slc", hw=(3, 4), strides=(1, 1), kw={}),
+        1: dict(z="slc_nan", hw=(3, 4), strides=(1, 1),
+                kw=dict(ps_mask="ps", nodata_mask="nodata", neighbor_arrays="nb11")),
+        2: dict(z="slc_nan", hw=(3, 4), strides=(2, 3),
+                kw=dict(ps_mask="ps", neighbor_arrays="nb23", use_max_ps=False, reference_idx=2,
+                        first_real_slc_idx=3, use_slc_amp=True)),
+        3: dict(z="slc", hw=(3, 4), strides=(1, 1),
+                kw=dict(use_evd=True, baseline_lag=3, beta=0.1, zero_correlation_threshold=0.05,
+                        ps_mask="ps", neighbor_arrays="nb11")),
+        4: dict(z="slc", hw=(3, 4), strides=(1, 1),
+                kw=dict(mask_input_ps=True, ps_mask="ps", avg_mag="mean", compute_crlb=False,
+                        reference_idx=-1)),
+        5: dict(z="slc", hw=(2, 2), strides=(3, 2),
+                kw=dict(ps_mask="ps", beta=0.05, first_real_slc_idx=1, baseline_lag=4)),
+    }
+    for idx, spec in specs.items():
+        kw = {k: (out[v] if isinstance(v, str) else v) for k, v in spec["kw"].items()}
+        if "ps_mask" in kw:
+            kw["ps_mask"] = kw["ps_mask"].copy()
+        if "nodata_mask" in kw:
+            kw["nodata_mask"] = kw["nodata_mask"].copy()
+        out.update(_pl_case(idx, out[spec["z"]], spec["hw"], spec["strides"], **kw))
+    meta = np.array([repr({k: (v["z"], v["hw"], v["strides"], v["kw"]) for k, v in specs.items()})])
+    _save("phase_link", specs=meta, **out)
+
+
+def make_config1_crop():
+    """Config-1 generator (N=10, gamma0=0.7, gamma_inf=0.1, tau=36 d) on a 40x48 crop."""
+    cfg = StackConfig(nslc=10, rows=40, cols=48, seed=20261204, ps_frac=0.05)
+    z = make_stack(cfg)
+    amp = np.abs(z)
+    mean, disp, ps = R.ps.calc_ps_block(amp.copy(), 0.25, cfg.nslc)
+    var = (disp * mean) ** 2
+    nb = np.asarray(
+        R.shp.estimate_neighbors(mean=mean, var=var, halfwin_rowcol=(5, 5), strides=ST(1, 1),
+                                 nslc=cfg.nslc, alpha=0.001, method="glrt"))
+    out = {"slc": z, "ps": ps, "mean": mean, "disp": disp, "var": var, "nb": nb}
+    out.update(_pl_case("emi", z, (5, 5), (1, 1), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean))
+    _save("config1_crop", **out)
+
+
+def make_ps_fill():
+    """get_max_idxs/fill_ps_pixels known answers, incl. the reference's strides-(3,6) regression layout."""
+    out = {}
+    ka = [
+        (np.array([[5, 1, 3], [4, 9, 2], [8, 7, 6]], dtype=np.float64), 1, 1),
+        (np.arange(16, dtype=np.float64).reshape(4, 4) + 1, 2, 2),
+        (np.array([[1, 5, 3], [4, 20, 2], [8, 0, 6]], dtype=np.float64), 2, 2),
+        (np.arange(9 * 11, dtype=np.float64).reshape(9, 11), 2, 3),
+    ]
+    for n in range(10, 15):
+        for looks in (2, 3):
+            ka.append((np.arange(n * n, dtype=np.float64).reshape(n, n), looks, looks))
+    for k, (arr, ry, rx) in enumerate(ka):
+        r, c = R.fill.get_max_idxs(arr, ry, rx)
+        out[f"ka_arr_{k}"], out[f"ka_looks_{k}"] = arr, np.array([ry, rx])
+        out[f"ka_r_{k}"], out[f"ka_c_{k}"] = np.asarray(r), np.asarray(c)
+    out["n_ka"] = np.array(len(ka))
+    # regression layout: PS positions of the reference's ps-fix fixture on a 522x534 grid
+    d = np.load("/root/reference/tests/data/ps-fix/failing_data_idxs.npz")
+    rows, cols = d["not_nan_rows"], d["not_nan_cols"]
+    rng = np.random.default_rng(601)
+    mags = (rng.normal(size=(522, 534)) ** 2).astype(np.float64)
+    avg_mag = np.full_like(mags, np.nan)
+    avg_mag[rows, cols] = mags[rows, cols]
+    r, c = R.fill.get_max_idxs(avg_mag, 3, 6)
+    out["fix_rows"], out["fix_cols"] = rows.astype(np.int16), cols.astype(np.int16)
+    out["fix_mags"] = mags[rows, cols]
+    out["fix_r"], out["fix_c"] = np.asarray(r).astype(np.int16), np.asarray(c).astype(np.int16)
+    _save("ps_fill", **out)
+
+
+if __name__ == "__main__":
+    which = sys.argv[1:] or ["ps", "glrt", "ks", "covariance", "phase_link", "config1", "ps_fill"]
+    for w in which:
+        print(f"[{w}]")
+        {"ps": make_ps, "glrt": make_glrt, "ks": make_ks, "covariance": make_covariance,
+         "phase_link": make_phase_link, "config1": make_config1_crop, "ps_fill": make_ps_fill}[w]()
