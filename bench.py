@@ -1,0 +1,370 @@
+"""Phase-linking benchmark: pixels/s on the 30-SLC 4096x4096 stack (EMI), 1024x1024 blocks.
+
+One step = the per-block hot path of dolphin's wrapped-phase workflow
+(workflows/single.py:215-294) over the whole frame: for each 1024x1024 block
+read with its (5, 11) halo, amplitude-dispersion PS selection, GLRT SHP
+selection (alpha 0.001) on the Rayleigh scale from the PS pass, and
+run_phase_linking (EMI, PS filling, CRLB), outputs trimmed to the block.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
+implementation instead (the numpy restatement of the reference algorithm:
+the reference itself needs jax/numba, which this environment lacks), over
+bounded crops of the same workload on all host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# ---- workload (config: 30 SLCs, 4096 x 4096, half-window (5, 11), GLRT 0.001, EMI) ----
+NSLC = 30
+FRAME = 4096
+BLOCK = 1024
+HALF = (5, 11)
+ALPHA = 0.001
+PS_THR = 0.25
+SEED = 20261205
+METRIC = "phase-linked pixels/sec (N=30, EMI) chosen vs plain GPU form at <=1e-3 rad; GB/s"
+UNIT = "pixels/s"
+
+
+def block_plan(rows, cols, block, half):
+    """Block slices with halo, as StridedBlockManager lays them out (io/_blocks.py:242-348).
+
+    Returns tuples (in_rows, in_cols, trim_rows, trim_cols, out_rows, out_cols): the
+    halo-padded input slice, the slice of the block result to keep, and where it goes.
+    """
+    hy, hx = half
+    plan = []
+    for r0 in range(0, rows, block):
+        r1 = min(rows, r0 + block)
+        for c0 in range(0, cols, block):
+            c1 = min(cols, c0 + block)
+            ir0, ir1 = max(0, r0 - hy), min(rows, r1 + hy)
+            ic0, ic1 = max(0, c0 - hx), min(cols, c1 + hx)
+            plan.append(((ir0, ir1), (ic0, ic1), (r0 - ir0, r1 - ir0), (c0 - ic0, c1 - ic0), (r0, r1), (c0, c1)))
+    return plan
+
+
+# ---------------------------------------------------------------------------------
+# CPU side (oracle restatement), run in spawned worker processes
+# ---------------------------------------------------------------------------------
+def _cpu_crop_worker(args):
+    seed, out_rows, out_cols = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    from dolphin_gb300.simulate import StackConfig, make_stack
+    from oracle import phase_link as O
+
+    hy, hx = HALF
+    cfg = StackConfig(nslc=NSLC, rows=out_rows + 2 * hy, cols=out_cols + 2 * hx, seed=seed, ps_frac=0.03)
+    z = make_stack(cfg)
+    t0 = time.perf_counter()
+    mean, disp, ps = O.calc_ps_block(np.abs(z), PS_THR, NSLC)
+    var = (disp * mean) ** 2
+    nb = O.estimate_neighbors_glrt(mean, var, HALF, (1, 1), NSLC, ALPHA)
+    O.run_phase_linking(z, HALF, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean)
+    dt = time.perf_counter() - t0
+    return out_rows * out_cols, dt
+
+
+def cpu_sample(pool, cores, crop=(64, 128), repeats=1):
+    """Time the CPU restatement on `cores` crops in parallel; returns (px/s, description)."""
+    jobs = [(SEED + 1000 + i, crop[0], crop[1]) for i in range(cores * repeats)]
+    t0 = time.perf_counter()
+    res = pool.map(_cpu_crop_worker, jobs)
+    wall = time.perf_counter() - t0
+    px = sum(r[0] for r in res)
+    desc = (f"{len(jobs)} crops of {crop[0]}x{crop[1]} output pixels (+halo) of the N=30 workload, "
+            f"one process per core, {wall:.1f}s wall")
+    return px / wall, desc
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = len(os.sched_getaffinity(0))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            cpu_sample(pool, cores, crop=(16, 32))
+        vals = []
+        descs = []
+        for _ in range(args.steps):
+            v, d = cpu_sample(pool, cores)
+            vals.append(v)
+            descs.append(d)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * FRAME * FRAME / value,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"N={NSLC} {FRAME}x{FRAME} stack, 1024x1024 blocks, half-window {HALF}, GLRT "
+                               f"{ALPHA}, EMI, PS {PS_THR} + fill, CRLB; bounded crops on CPU"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": descs[-1] + " (numpy restatement of the reference algorithm; the "
+                                               "reference needs jax/numba, absent here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in out.strip().splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[2:6]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def gpu_step(stack, plan, dp, outputs):
+    """One pass of the hot path over every block of a device-resident stack."""
+    cpx_full, tc_full = outputs
+    for (ir, ic, tr, tcl, orr, occ) in plan:
+        blk = stack[:, ir[0]:ir[1], ic[0]:ic[1]].contiguous()
+        mean, disp, ps = dp.calc_ps_block(blk.abs(), PS_THR, NSLC)
+        var = (disp * mean) ** 2
+        nb = dp.estimate_neighbors(halfwin_rowcol=HALF, alpha=ALPHA, mean=mean, var=var, nslc=NSLC)
+        out = dp.run_phase_linking(blk, HALF, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, compute_crlb=True)
+        cpx_full[:, orr[0]:orr[1], occ[0]:occ[1]] = out.cpx_phase[:, tr[0]:tr[1], tcl[0]:tcl[1]]
+        tc_full[orr[0]:orr[1], occ[0]:occ[1]] = out.temp_coh[tr[0]:tr[1], tcl[0]:tcl[1]]
+
+
+def run_ours(args, rank, world, pool, cores):
+    import torch
+
+    import dolphin_gb300 as dp
+    from dolphin_gb300 import _lib
+    from dolphin_gb300._build import build_library
+    from dolphin_gb300.simulate import StackConfig, make_stack_torch
+
+    build_library()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    frame = args.frame
+    cfg = StackConfig(nslc=NSLC, rows=frame, cols=frame, seed=SEED + rank, ps_frac=0.03)
+    stack = make_stack_torch(cfg, device=dev)
+    plan = block_plan(frame, frame, BLOCK, HALF)
+    cpx_full = torch.empty((NSLC, frame, frame), dtype=torch.complex64, device=dev)
+    tc_full = torch.empty((frame, frame), dtype=torch.float32, device=dev)
+    lib = _lib.load()
+
+    for _ in range(args.warmup):
+        gpu_step(stack, plan, dp, (cpx_full, tc_full))
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    sampler = ClockSampler(local)
+    sampler.start()
+    tot = _lib.C.c_double()
+    cnt = _lib.C.c_int64()
+    lib.dpl_kernel_timing(1, tot, cnt)
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        gpu_step(stack, plan, dp, (cpx_full, tc_full))
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    lib.dpl_kernel_timing(0, tot, cnt)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    kern_ms = tot.value / max(cnt.value, 1)
+    kern_launches_per_step = cnt.value / args.steps
+
+    # ---- end-to-end: pinned host stack in, host results out, through the public API ----
+    host_stack = torch.empty(stack.shape, dtype=stack.dtype, pin_memory=True)
+    host_stack.copy_(stack)
+    host_cpx = torch.empty(cpx_full.shape, dtype=cpx_full.dtype, pin_memory=True)
+    host_tc = torch.empty(tc_full.shape, dtype=tc_full.dtype, pin_memory=True)
+    del stack
+    torch.cuda.empty_cache()
+    dstack = torch.empty(host_stack.shape, dtype=host_stack.dtype, device=dev)
+
+    def e2e_step():
+        dstack.copy_(host_stack, non_blocking=True)
+        gpu_step(dstack, plan, dp, (cpx_full, tc_full))
+        host_cpx.copy_(cpx_full, non_blocking=True)
+        host_tc.copy_(tc_full, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e_step()
+    f1.record()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = f0.elapsed_time(f1) / e2e_steps
+    h2d = host_stack.numel() * host_stack.element_size()
+    d2h = host_cpx.numel() * host_cpx.element_size() + host_tc.numel() * host_tc.element_size()
+
+    # max over ranks
+    vals = torch.tensor([ms, e2e_ms, kern_ms], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    ms, e2e_ms, kern_ms = vals.tolist()
+    if rank != 0:
+        return
+    px = frame * frame * world
+    value = px / (ms / 1000.0)
+    # roofline of the dominant kernel (per-pixel covariance + solver): algorithmic flops
+    W = (2 * HALF[0] + 1) * (2 * HALF[1] + 1)
+    f_cov = 4.0 * W * NSLC * (NSLC + 1)
+    px_per_launch = sum((ir[1] - ir[0]) * (ic[1] - ic[0]) for (ir, ic, *_r) in plan) / len(plan)
+    achieved = f_cov * px_per_launch / (kern_ms / 1000.0) / 1e12
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    cpu = None
+    if pool is not None:
+        cv, cd = cpu_sample(pool, cores)
+        cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": cd + " (numpy restatement of the reference algorithm)"}
+    launches_per_step = len(plan) * 6  # k_ps_block, k_glrt_scale, k_glrt, k_prep, k_pixel, k_post
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"N={NSLC} {frame}x{frame} stack per GPU, {BLOCK}x{BLOCK} blocks with halo, "
+                               f"half-window {HALF}, GLRT {ALPHA}, EMI, PS {PS_THR} + fill, CRLB",
+                   "l2": "inputs larger than L2 (4 GB stack per GPU)", "form": "plain (FP32 SIMT covariance)"},
+        "e2e": {"value": px / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches_per_step * args.steps),
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_pixel", "kernel_ms": kern_ms,
+                     "launches_per_step": kern_launches_per_step,
+                     "note": "algorithmic covariance flops 4*W*N*(N+1) per pixel over the measured launch time; "
+                             "peak = measured bf16 dense (MEASURED_PEAKS.json)"},
+        "clocks": clocks,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frame", type=int, default=FRAME)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    pool = None
+    cores = len(os.sched_getaffinity(0))
+    if rank == 0 and not args.no_cpu:
+        # start the CPU worker pool (spawn) before the first CUDA call
+        pool = mp.get_context("spawn").Pool(cores)
+    try:
+        run_ours(args, rank, world, pool, cores)
+    finally:
+        if pool is not None:
+            pool.terminate()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1095 @@
+// Phase linking: run_phase_linking (phase_link/_core.py:67-249) on one GPU.
+//
+// Pipeline (one stream, no host round trip until the final status check):
+//   k_prep   -- per input pixel: nodata |= any NaN, ps &= !nodata, the masked stack
+//               (NaN and ignored pixels -> 0, the reference's `where(mask, z, 0)`)
+//               transposed to pixel-major (rows, cols, N), nanmean|z| if needed, and a
+//               per-SLC "has a non-NaN sample" bitmask for the all-NaN check.
+//   k_pixel  -- one warp per output pixel, matrices in the warp's shared memory:
+//               SHP-masked sample coherence (covariance.py:110-142), baseline lag
+//               (_core.py:333-337), closure phases (_closure_phase.py:6-40),
+//               |Gamma| regularisation and Cholesky inverse (_core.py:452-472),
+//               EMI by LU + inverse iteration (_eigenvalues.py:139-205) or EVD by
+//               power iteration (:93-136) with the reference's per-pixel fallback,
+//               referencing (_core.py:530-534), temporal coherence (metrics.py:74-97)
+//               and CRLB (crlb.py:132-189).  Written pixel-major.
+//   k_post   -- per output pixel: unit phasors, PS filling (_ps_filling.py:16-97),
+//               use_slc_amp, nodata NaNs (_core.py:207-238), transposed to the
+//               reference's (N, rows, cols) output layout.
+//
+// Precision: float32 throughout, as in the reference (jax with x64 disabled).
+// Iteration caps and tolerances are the reference's (<= 49 iterations, 1e-5).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <sstream>
+#include <vector>
+
+#include "dpl_common.cuh"
+
+namespace dpl {
+
+__device__ __forceinline__ int clamp_start_i(int center, int half, int size, int dim) {
+    int s = center - half;
+    s = s < 0 ? 0 : s;
+    return s > dim - size ? dim - size : s;
+}
+
+// ---------------------------------------------------------------------------------
+// k_prep
+// ---------------------------------------------------------------------------------
+constexpr int kPrepPix = 64;
+
+__global__ void __launch_bounds__(256) k_prep(const cfloat* __restrict__ slc, int n, int64_t npix,
+                                              const uint8_t* __restrict__ nodata_in,
+                                              const uint8_t* __restrict__ ps_in, int mask_input_ps,
+                                              uint8_t* __restrict__ flags, cfloat* __restrict__ zt,
+                                              float* __restrict__ avgmag, unsigned int* __restrict__ valid_bits) {
+    extern __shared__ cfloat prep_s[];  // [kPrepPix][n + 1]
+    __shared__ uint8_t ign[kPrepPix];
+    __shared__ unsigned long long vbits;
+    const int ld = n + 1;
+    const int64_t p0 = (int64_t)blockIdx.x * kPrepPix;
+    if (threadIdx.x == 0) vbits = 0ull;
+    for (int i = threadIdx.x; i < n * kPrepPix; i += blockDim.x) {
+        const int t = i / kPrepPix, px = i - t * kPrepPix;
+        const int64_t p = p0 + px;
+        prep_s[px * ld + t] = p < npix ? slc[(int64_t)t * npix + p] : cmake(0.f, 0.f);
+    }
+    __syncthreads();
+    if (threadIdx.x < kPrepPix) {
+        const int px = threadIdx.x;
+        const int64_t p = p0 + px;
+        if (p < npix) {
+            bool anynan = false;
+            unsigned long long vb = 0ull;
+            float msum = 0.f;
+            int mcnt = 0;
+            for (int t = 0; t < n; ++t) {
+                cfloat z = prep_s[px * ld + t];
+                bool nan = cisnan(z);
+                anynan |= nan;
+                if (!nan) {
+                    vb |= 1ull << t;
+                    float m = hypotf(z.re, z.im);
+                    msum = mcnt == 0 ? m : fadd(msum, m);
+                    ++mcnt;
+                }
+            }
+            const bool nodata = (nodata_in && nodata_in[p]) || anynan;
+            const bool ps = ps_in && ps_in[p] && !nodata;
+            const bool ignore = nodata || (mask_input_ps && ps);
+            flags[p] = (nodata ? kNodata : 0) | (ps ? kPs : 0) | (ignore ? kIgnore : 0);
+            ign[px] = ignore;
+            if (avgmag) avgmag[p] = fdiv(msum, (float)mcnt);
+            if (vb) atomicOr(&vbits, vb);
+        } else {
+            ign[px] = 1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && vbits) {
+        atomicOr(valid_bits, (unsigned int)(vbits & 0xffffffffull));
+        atomicOr(valid_bits + 1, (unsigned int)(vbits >> 32));
+    }
+    for (int i = threadIdx.x; i < kPrepPix * n; i += blockDim.x) {
+        const int px = i / n, t = i - px * n;
+        const int64_t p = p0 + px;
+        if (p < npix) {
+            cfloat z = prep_s[px * ld + t];
+            if (ign[px] || cisnan(z)) z = cmake(0.f, 0.f);
+            zt[p * n + t] = z;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// k_pixel: per-warp shared-memory layout
+// ---------------------------------------------------------------------------------
+struct PixLayout {
+    int n, ldm, ldg, np, stg;  // stg: staging length (complex) for one window row
+    size_t off_C, off_G, off_Gi, off_LU, off_v, off_d, off_perm, bytes;
+};
+
+inline PixLayout make_layout(int n, int wx) {
+    PixLayout L{};
+    L.n = n;
+    L.ldm = n | 1;
+    L.ldg = n | 1;
+    L.np = (n + 1) & ~1;
+    L.stg = wx * L.np + 32;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = align_up(o + bytes, 16);
+        return at;
+    };
+    L.off_C = take((size_t)n * L.ldm * sizeof(cfloat));
+    L.off_G = take((size_t)n * L.ldg * sizeof(float));
+    L.off_Gi = take((size_t)n * L.ldg * sizeof(float));
+    L.off_LU = take(std::max((size_t)n * L.ldm, (size_t)L.stg) * sizeof(cfloat));
+    L.off_v = take(64 * sizeof(cfloat));
+    L.off_d = take(64 * sizeof(float));
+    L.off_perm = take(128 * sizeof(int));  // pivots [0, 64) and their permutation [64, 128)
+    L.bytes = align_up(o, 128);
+    return L;
+}
+
+enum PixMode { kCovOnly = 0, kSolveOnly = 1, kFused = 2 };
+
+struct PixArgs {
+    int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
+    int64_t npix;
+    int ldm, ldg, np, stg;
+    size_t off_C, off_G, off_Gi, off_LU, off_v, off_d, off_perm, warp_bytes;
+    const cfloat* zt;        // (rows, cols, n) masked, pixel-major
+    const uint8_t* nb_u8;    // (out_rows, out_cols, wy, wx) or null
+    const uint32_t* nb_bits; // (out_rows, out_cols, wy, wpr) or null
+    int wpr;
+    const cfloat* Cin;       // solve-only input: (npix, n, n)
+    int use_evd, beta_on;
+    float one_minus_beta, beta, zct;
+    int ref_idx, compute_crlb, crlb_ref, baseline_lag;
+    float crlb_factor;
+    cfloat* Cout;            // cov-only output: (npix, n, n)
+    cfloat* vout;            // (npix, n) referenced eigenvectors
+    float* eig;
+    uint8_t* est;
+    float* crlb;             // (npix, n)
+    float* tcoh;
+    float* closure;          // (npix, n - 2) or null
+    int32_t* counts;         // (npix) or null
+};
+
+struct Mats {
+    cfloat* C;
+    float* G;
+    float* Gi;
+    cfloat* LU;
+    cfloat* v;
+    float* d;
+    int* perm;
+};
+
+// ---------------------------------------------------------------------------------
+// covariance (covariance.py:110-170): raw sums into C, then normalisation
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t row_mask(const PixArgs& a, int64_t p, int wa, int wx, int lane) {
+    const uint64_t full = wx >= 64 ? ~0ull : ((1ull << wx) - 1ull);
+    if (a.nb_bits) {
+        const uint32_t* w = a.nb_bits + ((p * (2 * a.hy + 1) + wa) * a.wpr);
+        uint64_t m = w[0];
+        if (a.wpr > 1) m |= (uint64_t)w[1] << 32;
+        return m & full;
+    }
+    if (a.nb_u8) {
+        const uint8_t* b = a.nb_u8 + (p * (2 * a.hy + 1) + wa) * wx;
+        uint32_t lo = __ballot_sync(0xffffffffu, lane < wx && b[lane] != 0);
+        uint32_t hi = __ballot_sync(0xffffffffu, lane + 32 < wx && b[lane + 32] != 0);
+        return ((uint64_t)hi << 32) | lo;
+    }
+    return full;
+}
+
+template <int NB>
+__device__ void warp_covariance(const PixArgs& a, int64_t p, const Mats& m, int lane, int* count_out) {
+    const int n = a.n, wy = 2 * a.hy + 1, wx = 2 * a.hx + 1, np = a.np;
+    const int out_r = (int)(p / a.out_cols), out_c = (int)(p - (int64_t)out_r * a.out_cols);
+    const int in_r = a.sy / 2 + out_r * a.sy, in_c = a.sx / 2 + out_c * a.sx;
+    const int r0 = clamp_start_i(in_r, a.hy, wy, a.rows), c0 = clamp_start_i(in_c, a.hx, wx, a.cols);
+    cfloat* stg = m.LU;
+    int count = 0;
+    for (int rb = 0; rb < NB; ++rb) {
+        for (int cb = rb; cb < NB; ++cb) {
+            float are[32], aim[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) are[j] = aim[j] = 0.f;
+            for (int wa = 0; wa < wy; ++wa) {
+                const uint64_t rm = row_mask(a, p, wa, wx, lane);
+                if (rb == 0 && cb == 0) count += __popcll(rm);
+                if (rm == 0ull) continue;
+                const cfloat* src = a.zt + ((int64_t)(r0 + wa) * a.cols + c0) * n;
+                for (int idx = lane; idx < a.stg; idx += 32) {
+                    const int b = idx / np, t = idx - b * np;
+                    stg[idx] = (b < wx && t < n) ? src[b * n + t] : cmake(0.f, 0.f);
+                }
+                __syncwarp();
+                for (int wb = 0; wb < wx; ++wb) {
+                    if (!((rm >> wb) & 1ull)) continue;
+                    const cfloat* s = stg + wb * np;
+                    const cfloat zi = s[rb * 32 + lane];
+                    const float4* sj = reinterpret_cast<const float4*>(s + cb * 32);
+#pragma unroll
+                    for (int j2 = 0; j2 < 16; ++j2) {
+                        const float4 q = sj[j2];
+                        are[2 * j2] += zi.re * q.x + zi.im * q.y;
+                        aim[2 * j2] += zi.im * q.x - zi.re * q.y;
+                        are[2 * j2 + 1] += zi.re * q.z + zi.im * q.w;
+                        aim[2 * j2 + 1] += zi.im * q.z - zi.re * q.w;
+                    }
+                }
+                __syncwarp();
+            }
+            const int row = rb * 32 + lane;
+            if (row < n) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int col = cb * 32 + j;
+                    if (col < n) {
+                        m.C[row * a.ldm + col] = cmake(are[j], aim[j]);
+                        if (rb != cb) m.C[col * a.ldm + row] = cmake(are[j], -aim[j]);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    // C = numer / sqrt(amp_i amp_j) where that root > 1e-6, else 0
+    for (int i = lane; i < n; i += 32) m.d[i] = m.C[i * a.ldm + i].re;
+    __syncwarp();
+    for (int e = lane; e < n * n; e += 32) {
+        const int i = e / n, j = e - i * n;
+        const float s = fsqrt(fmul(m.d[i], m.d[j]));
+        cfloat c = m.C[i * a.ldm + j];
+        m.C[i * a.ldm + j] = s > 1e-6f ? cmake(fdiv(c.re, s), fdiv(c.im, s)) : cmake(0.f, 0.f);
+    }
+    __syncwarp();
+    if (count_out) *count_out = count;
+}
+
+// ---------------------------------------------------------------------------------
+// dense per-warp linear algebra
+// ---------------------------------------------------------------------------------
+// Cholesky (lower, right-looking) in place; returns false on a non-positive pivot.
+__device__ bool warp_cholesky(float* G, int ldg, int n, int lane) {
+    for (int k = 0; k < n; ++k) {
+        const float dkk = G[k * ldg + k];
+        if (!(dkk > 0.f)) return false;  // uniform: every lane read the same value
+        const float lkk = fsqrt(dkk);
+        __syncwarp();
+        if (lane == 0) G[k * ldg + k] = lkk;
+        for (int i = k + 1 + lane; i < n; i += 32) G[i * ldg + k] = fdiv(G[i * ldg + k], lkk);
+        __syncwarp();
+        for (int i = k + 1 + lane; i < n; i += 32) {
+            const float lik = G[i * ldg + k];
+            for (int j = k + 1; j <= i; ++j) G[i * ldg + j] -= lik * G[j * ldg + k];
+        }
+        __syncwarp();
+    }
+    return true;
+}
+
+// Y = L^{-1} (lower) by column-parallel forward substitution.  If sumsq is non-null,
+// lane-owned columns also return sum_k Y[k][j]^2 (the diagonal of (L L^T)^{-1}).
+__device__ void warp_tri_inverse(const float* L, float* Y, int ldg, int n, int lane, float* sumsq) {
+    for (int j = lane; j < n; j += 32) {
+        const float yjj = fdiv(1.f, L[j * ldg + j]);
+        Y[j * ldg + j] = yjj;
+        float ss = yjj * yjj;
+        for (int i = j + 1; i < n; ++i) {
+            float s = 0.f;
+            for (int k = j; k < i; ++k) s += L[i * ldg + k] * Y[k * ldg + j];
+            const float yij = -fdiv(s, L[i * ldg + i]);
+            Y[i * ldg + j] = yij;
+            ss += yij * yij;
+        }
+        if (sumsq) sumsq[j] = ss;
+    }
+    __syncwarp();
+}
+
+// LU with partial pivoting (getrf: pivot = first maximum of |re| + |im|), in place.
+__device__ void warp_lu(cfloat* A, int ldm, int n, int* piv, int lane) {
+    for (int k = 0; k < n; ++k) {
+        float best = -1.f;
+        int bi = n;
+        for (int i = k + lane; i < n; i += 32) {
+            const cfloat x = A[i * ldm + k];
+            const float v = fabsf(x.re) + fabsf(x.im);
+            if (v > best) {
+                best = v;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if (bi >= n) bi = k;
+        if (lane == 0) piv[k] = bi;
+        if (bi != k) {
+            for (int j = lane; j < n; j += 32) {
+                const cfloat t = A[k * ldm + j];
+                A[k * ldm + j] = A[bi * ldm + j];
+                A[bi * ldm + j] = t;
+            }
+        }
+        __syncwarp();
+        const cfloat pv = A[k * ldm + k];
+        if (pv.re != 0.f || pv.im != 0.f) {
+            const cfloat r = cdiv(cmake(1.f, 0.f), pv);
+            for (int i = k + 1 + lane; i < n; i += 32) A[i * ldm + k] = cmul(A[i * ldm + k], r);
+        }
+        __syncwarp();
+        for (int i = k + 1 + lane; i < n; i += 32) {
+            const cfloat lik = A[i * ldm + k];
+            for (int j = k + 1; j < n; ++j) A[i * ldm + j] = csub(A[i * ldm + j], cmul(lik, A[k * ldm + j]));
+        }
+        __syncwarp();
+    }
+}
+
+template <int NB>
+__device__ __forceinline__ cfloat bcast(const cfloat (&x)[NB], int k) {
+    cfloat r = shfl_c(x[0], k & 31);
+    if (NB > 1) {
+        cfloat r1 = shfl_c(x[NB - 1], k & 31);
+        if (k >= 32) r = r1;
+    }
+    return r;
+}
+
+template <int NB>
+__device__ __forceinline__ float vnorm2(const cfloat (&x)[NB]) {
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) s += cabs2(x[q]);
+    return warp_sum(s);
+}
+
+// x <- (LU)^{-1} P x   (lu_solve: row interchanges, unit-lower then upper solve)
+template <int NB>
+__device__ void warp_lu_solve(const cfloat* A, int ldm, int n, const int* perm, cfloat (&x)[NB], int lane) {
+    cfloat w[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        const int i = lane + 32 * q;
+        const int src = i < n ? perm[i] : 0;
+        cfloat t0 = shfl_c(x[0], src & 31);
+        cfloat t1 = NB > 1 ? shfl_c(x[NB - 1], src & 31) : t0;
+        w[q] = (i < n) ? ((src >= 32) ? t1 : t0) : cmake(0.f, 0.f);
+    }
+    for (int k = 0; k < n - 1; ++k) {
+        const cfloat xk = bcast<NB>(w, k);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int i = lane + 32 * q;
+            if (i > k && i < n) w[q] = csub(w[q], cmul(A[i * ldm + k], xk));
+        }
+    }
+    for (int k = n - 1; k >= 0; --k) {
+#pragma unroll
+        for (int q = 0; q < NB; ++q)
+            if (lane + 32 * q == k) w[q] = cdiv(w[q], A[k * ldm + k]);
+        const cfloat xk = bcast<NB>(w, k);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int i = lane + 32 * q;
+            if (i < k) w[q] = csub(w[q], cmul(A[i * ldm + k], xk));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) x[q] = w[q];
+}
+
+// y = M x with M[i][j] = B[i][j] (complex matrix in smem)
+template <int NB>
+__device__ void warp_matvec(const cfloat* B, int ldm, int n, const cfloat (&x)[NB], cfloat (&y)[NB], int lane) {
+#pragma unroll
+    for (int q = 0; q < NB; ++q) y[q] = cmake(0.f, 0.f);
+    for (int j = 0; j < n; ++j) {
+        const cfloat xj = bcast<NB>(x, j);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int i = lane + 32 * q;
+            if (i < n) y[q] = cadd(y[q], cmul(B[i * ldm + j], xj));
+        }
+    }
+}
+
+// Re(v^H A v) with A = Gi o C (real weights times complex entries)
+template <int NB>
+__device__ float warp_rayleigh_weighted(const float* W, int ldg, const cfloat* C, int ldm, int n,
+                                        const cfloat (&v)[NB], int lane) {
+    cfloat y[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) y[q] = cmake(0.f, 0.f);
+    for (int j = 0; j < n; ++j) {
+        const cfloat vj = bcast<NB>(v, j);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int i = lane + 32 * q;
+            if (i < n) y[q] = cadd(y[q], cmul(cscale(C[i * ldm + j], W[i * ldg + j]), vj));
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) s += v[q].re * y[q].re + v[q].im * y[q].im;
+    return warp_sum(s);
+}
+
+template <int NB>
+__device__ float warp_rayleigh(const cfloat* B, int ldm, int n, const cfloat (&v)[NB], int lane) {
+    cfloat y[NB];
+    warp_matvec<NB>(B, ldm, n, v, y, lane);
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) s += v[q].re * y[q].re + v[q].im * y[q].im;
+    return warp_sum(s);
+}
+
+// ---------------------------------------------------------------------------------
+// solver (process_coherence_matrices + temporal coherence + closure phases)
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ float gamma_reg(const PixArgs& a, const cfloat* C, int ldm, int i, int j) {
+    float g = cabs(C[i * ldm + j]);
+    if (a.beta_on) g = fadd(fmul(a.one_minus_beta, g), i == j ? a.beta : 0.f);
+    return g < a.zct ? 0.f : g;
+}
+
+template <int NB>
+__device__ void warp_solve(const PixArgs& a, int64_t p, const Mats& m, int lane) {
+    const int n = a.n, ldm = a.ldm, ldg = a.ldg;
+    cfloat* C = m.C;
+    if (a.baseline_lag > 0) {
+        for (int e = lane; e < n * n; e += 32) {
+            const int i = e / n, j = e - i * n;
+            if (abs(i - j) >= a.baseline_lag) C[i * ldm + j] = cmake(0.f, 0.f);
+        }
+        __syncwarp();
+    }
+    if (a.closure) {
+        for (int i = lane; i < n - 2; i += 32) {
+            const cfloat c = cmulc(cmul(C[i * ldm + i + 1], C[(i + 1) * ldm + i + 2]), C[i * ldm + i + 2]);
+            a.closure[p * (n - 2) + i] = atan2f(c.im, c.re);
+        }
+    }
+    // |Gamma| (+ regularisation) + 1e-6 I, Cholesky, inverse
+    float* G = m.G;
+    for (int e = lane; e < n * n; e += 32) {
+        const int i = e / n, j = e - i * n;
+        if (j <= i) G[i * ldg + j] = fadd(gamma_reg(a, C, ldm, i, j), i == j ? 1e-6f : 0.f);
+    }
+    __syncwarp();
+    const bool chol_ok = warp_cholesky(G, ldg, n, lane);
+    __syncwarp();
+    bool inv_nan;
+    if (chol_ok) {
+        warp_tri_inverse(G, m.Gi, ldg, n, lane, nullptr);
+        bool bad = false;
+        for (int e = lane; e < n * n; e += 32) {
+            const int i = e / n, j = e - i * n;
+            if (i <= j) {
+                float s = 0.f;
+                for (int k = j; k < n; ++k) s += m.Gi[k * ldg + i] * m.Gi[k * ldg + j];
+                G[i * ldg + j] = s;
+                G[j * ldg + i] = s;
+                bad |= isnan(s);
+            }
+        }
+        inv_nan = warp_any(bad);
+    } else {
+        for (int e = lane; e < n * n; e += 32) G[(e / n) * ldg + (e % n)] = nanf("");
+        inv_nan = true;
+    }
+    __syncwarp();
+
+    cfloat v[NB];
+    float lambda;
+    const bool evd = a.use_evd || inv_nan;
+    cfloat* LU = m.LU;
+    const float inv_sqrt_n = fdiv(1.f, fsqrt((float)n));
+#pragma unroll
+    for (int q = 0; q < NB; ++q) v[q] = (lane + 32 * q < n) ? cmake(inv_sqrt_n, 0.f) : cmake(0.f, 0.f);
+    if (!evd) {
+        // EMI: inverse iteration on (|Gamma|^-1 o C) - 0.99 I
+        for (int e = lane; e < n * n; e += 32) {
+            const int i = e / n, j = e - i * n;
+            cfloat x = cscale(C[i * ldm + j], G[i * ldg + j]);
+            if (i == j) x.re = fsub(x.re, 0.99f);
+            LU[i * ldm + j] = x;
+        }
+        __syncwarp();
+        warp_lu(LU, ldm, n, m.perm + 0, lane);
+        // permutation of the row interchanges (lane 0), stored after the pivots
+        int* perm = m.perm + 64;
+        if (lane == 0) {
+            for (int i = 0; i < n; ++i) perm[i] = i;
+            for (int k = 0; k < n; ++k) {
+                const int pk = m.perm[k];
+                const int t = perm[k];
+                perm[k] = perm[pk];
+                perm[pk] = t;
+            }
+        }
+        __syncwarp();
+        float diff = 1.f;
+        for (int it = 1; diff > 1e-5f && it < 50; ++it) {
+            cfloat x[NB];
+#pragma unroll
+            for (int q = 0; q < NB; ++q) x[q] = v[q];
+            warp_lu_solve<NB>(LU, ldm, n, perm, x, lane);
+            const float nrm = fsqrt(vnorm2<NB>(x));
+            float dd = 0.f;
+#pragma unroll
+            for (int q = 0; q < NB; ++q) {
+                x[q] = cmake(fdiv(x[q].re, nrm), fdiv(x[q].im, nrm));
+                dd += cabs2(csub(x[q], v[q]));
+                v[q] = x[q];
+            }
+            diff = fsqrt(warp_sum(dd));
+        }
+        lambda = warp_rayleigh_weighted<NB>(G, ldg, C, ldm, n, v, lane);
+        const float scale = fdiv(fsqrt((float)n), fsqrt(vnorm2<NB>(v)));
+#pragma unroll
+        for (int q = 0; q < NB; ++q) v[q] = cscale(v[q], scale);
+    } else {
+        // EVD: power iteration on C o |C|
+        for (int e = lane; e < n * n; e += 32) {
+            const int i = e / n, j = e - i * n;
+            const cfloat c = C[i * ldm + j];
+            LU[i * ldm + j] = cscale(c, cabs(c));
+        }
+        __syncwarp();
+        float diff = 1.f;
+        for (int it = 1; diff > 1e-5f && it < 50; ++it) {
+            cfloat y[NB];
+            warp_matvec<NB>(LU, ldm, n, v, y, lane);
+            const float nrm = fsqrt(vnorm2<NB>(y));
+            float dd = 0.f;
+#pragma unroll
+            for (int q = 0; q < NB; ++q) {
+                y[q] = cmake(fdiv(y[q].re, nrm), fdiv(y[q].im, nrm));
+                dd += cabs2(csub(y[q], v[q]));
+                v[q] = y[q];
+            }
+            diff = fsqrt(warp_sum(dd));
+        }
+        lambda = warp_rayleigh<NB>(LU, ldm, n, v, lane);
+    }
+    // reference to reference_idx: v * exp(-i angle(v[ref]))
+    const cfloat vr = bcast<NB>(v, a.ref_idx);
+    const cfloat rot = cconj(cphasor(vr));
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        const int i = lane + 32 * q;
+        if (i < n) {
+            v[q] = cmul(v[q], rot);
+            m.v[i] = v[q];
+            a.vout[p * n + i] = v[q];
+        }
+    }
+    if (lane == 0) {
+        a.eig[p] = lambda;
+        a.est[p] = evd ? 0 : 1;
+    }
+    __syncwarp();
+    // temporal coherence over i < j (metrics.py:74-97, unit weights)
+    {
+        float sre = 0.f, sim = 0.f;
+        int cnt = 0;
+        for (int i = 0; i < n - 1; ++i) {
+            const cfloat vi = m.v[i];
+            for (int j = i + 1 + lane; j < n; j += 32) {
+                const cfloat u = cphasor(C[i * ldm + j]);
+                const cfloat w = cphasor(cmulc(vi, m.v[j]));
+                const cfloat t = cmulc(u, w);
+                if (!cisnan(t)) {
+                    sre += t.re;
+                    sim += t.im;
+                    ++cnt;
+                }
+            }
+        }
+        sre = warp_sum(sre);
+        sim = warp_sum(sim);
+        cnt = warp_sum_int(cnt);
+        if (lane == 0) {
+            const float fc = (float)cnt;
+            float tc = hypotf(fdiv(sre, fc), fdiv(sim, fc));
+            a.tcoh[p] = isfinite(tc) ? tc : 0.f;
+        }
+    }
+    // CRLB (crlb.py:132-189): X = 2L (Gamma o Gamma^-1 - I), drop `ref`, + 1e-6 I,
+    // sigma = sqrt(diag(FIM^-1)) with 0 inserted at `ref`
+    if (a.compute_crlb) {
+        const int ref = a.crlb_ref, mm = n - 1;
+        float* F = reinterpret_cast<float*>(LU);
+        __syncwarp();
+        for (int e = lane; e < mm * mm; e += 32) {
+            const int ii = e / mm, jj = e - ii * mm;
+            if (jj > ii) continue;
+            const int i = ii + (ii >= ref), j = jj + (jj >= ref);
+            const float x = fmul(a.crlb_factor, fsub(fmul(gamma_reg(a, C, ldm, i, j), G[i * ldg + j]), i == j ? 1.f : 0.f));
+            F[ii * ldg + jj] = ii == jj ? fadd(x, 1e-6f) : x;
+        }
+        __syncwarp();
+        const bool ok = mm > 0 && warp_cholesky(F, ldg, mm, lane);
+        __syncwarp();
+        if (ok) warp_tri_inverse(F, m.Gi, ldg, mm, lane, m.d);
+        __syncwarp();
+        for (int t = lane; t < n; t += 32) {
+            float sg;
+            if (t == ref) sg = 0.f;
+            else sg = ok ? fsqrt(m.d[t - (t > ref)]) : nanf("");
+            a.crlb[p * n + t] = sg;
+        }
+    } else {
+        for (int t = lane; t < n; t += 32) a.crlb[p * n + t] = 0.f;
+    }
+    __syncwarp();
+}
+
+template <int NB, int MODE>
+__global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
+    extern __shared__ __align__(16) unsigned char pix_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    unsigned char* base = pix_smem + warp * a.warp_bytes;
+    Mats m;
+    m.C = reinterpret_cast<cfloat*>(base + a.off_C);
+    m.G = reinterpret_cast<float*>(base + a.off_G);
+    m.Gi = reinterpret_cast<float*>(base + a.off_Gi);
+    m.LU = reinterpret_cast<cfloat*>(base + a.off_LU);
+    m.v = reinterpret_cast<cfloat*>(base + a.off_v);
+    m.d = reinterpret_cast<float*>(base + a.off_d);
+    m.perm = reinterpret_cast<int*>(base + a.off_perm);
+    for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
+        if (MODE == kSolveOnly) {
+            const cfloat* src = a.Cin + p * a.n * a.n;
+            for (int e = lane; e < a.n * a.n; e += 32) m.C[(e / a.n) * a.ldm + (e % a.n)] = src[e];
+            __syncwarp();
+        } else {
+            int count = 0;
+            warp_covariance<NB>(a, p, m, lane, &count);
+            if (a.counts && lane == 0) a.counts[p] = count;
+        }
+        if (MODE == kCovOnly) {
+            cfloat* dst = a.Cout + p * a.n * a.n;
+            for (int e = lane; e < a.n * a.n; e += 32) dst[e] = m.C[(e / a.n) * a.ldm + (e % a.n)];
+            __syncwarp();
+        } else {
+            warp_solve<NB>(a, p, m, lane);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// k_post: phasors, PS fill, use_slc_amp, nodata, transposition to (N, rows, cols)
+// ---------------------------------------------------------------------------------
+struct PostArgs {
+    int n, rows, cols, sy, sx, out_rows, out_cols;
+    const cfloat* slc;  // original stack (N, rows, cols)
+    const uint8_t* flags;
+    const float* mag;   // brightness for the PS argmax (avg_mag or nanmean |slc|)
+    const cfloat* V;    // (P, n) referenced eigenvectors
+    const float* CR;    // (P, n)
+    int use_max_ps, use_slc_amp, ref_idx;
+    cfloat* cpx;        // (n, P)
+    float* tcoh;        // (P), in/out
+    float* crlb;        // (n, P)
+    int* status;
+};
+
+__global__ void __launch_bounds__(256) k_post(PostArgs a) {
+    const int64_t P = (int64_t)a.out_rows * a.out_cols;
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int orow = (int)(p / a.out_cols), ocol = (int)(p - (int64_t)orow * a.out_cols);
+    const int64_t npix_in = (int64_t)a.rows * a.cols;
+    bool all_nodata = true, any_ps = false;
+    float best = -INFINITY;
+    int br = -1, bc = -1, nps = 0;
+    for (int dr = 0; dr < a.sy; ++dr) {
+        for (int dc = 0; dc < a.sx; ++dc) {
+            const int r = orow * a.sy + dr, c = ocol * a.sx + dc;
+            const uint8_t f = a.flags[(int64_t)r * a.cols + c];
+            all_nodata &= (f & kNodata) != 0;
+            if (f & kPs) {
+                any_ps = true;
+                ++nps;
+                const float mg = a.mag[(int64_t)r * a.cols + c];
+                if (!isnan(mg) && mg > best) {
+                    best = mg;
+                    br = r;
+                    bc = c;
+                }
+            }
+        }
+    }
+    if (any_ps && a.use_max_ps && br < 0) atomicExch(a.status, (int)DPL_ERR_INVALID_ARGUMENT);
+    const int in_r = a.sy / 2 + orow * a.sy, in_c = a.sx / 2 + ocol * a.sx;
+    for (int t = 0; t < a.n; ++t) {
+        cfloat out = cphasor(a.V[p * a.n + t]);
+        if (any_ps) {
+            const float amp = cabs(out);
+            if (a.use_max_ps) {
+                if (br >= 0) {
+                    const cfloat zt = a.slc[(int64_t)t * npix_in + (int64_t)br * a.cols + bc];
+                    const cfloat zr = a.slc[(int64_t)a.ref_idx * npix_in + (int64_t)br * a.cols + bc];
+                    out = cscale(cmul(cphasor(zt), cconj(cphasor(zr))), amp);
+                }
+            } else {
+                float sre = 0.f, sim = 0.f;
+                int cnt = 0;
+                for (int dr = 0; dr < a.sy; ++dr) {
+                    for (int dc = 0; dc < a.sx; ++dc) {
+                        const int r = orow * a.sy + dr, c = ocol * a.sx + dc;
+                        if (!(a.flags[(int64_t)r * a.cols + c] & kPs)) continue;
+                        const int64_t q = (int64_t)r * a.cols + c;
+                        const cfloat z = cmul(a.slc[(int64_t)t * npix_in + q], cconj(cphasor(a.slc[q])));
+                        if (cisnan(z)) continue;
+                        sre += z.re;
+                        sim += z.im;
+                        ++cnt;
+                    }
+                }
+                const cfloat avg = cmake(fdiv(sre, (float)cnt), fdiv(sim, (float)cnt));
+                out = cscale(cphasor(avg), amp);
+            }
+        }
+        if (a.use_slc_amp) {
+            const cfloat z = a.slc[(int64_t)t * npix_in + (int64_t)in_r * a.cols + in_c];
+            out = cscale(cphasor(out), cabs(z));
+        }
+        if (all_nodata) out = cmake(nanf(""), 0.f);
+        a.cpx[(int64_t)t * P + p] = out;
+        a.crlb[(int64_t)t * P + p] = a.CR[p * a.n + t];
+    }
+    float tc = a.tcoh[p];
+    if (any_ps) tc = 1.f;
+    if (all_nodata) tc = nanf("");
+    a.tcoh[p] = tc;
+}
+
+// ---------------------------------------------------------------------------------
+// host
+// ---------------------------------------------------------------------------------
+static void fill_pix_layout(PixArgs& a, int n, int wx) {
+    PixLayout L = make_layout(n, wx);
+    a.n = n;
+    a.ldm = L.ldm;
+    a.ldg = L.ldg;
+    a.np = L.np;
+    a.stg = L.stg;
+    a.off_C = L.off_C;
+    a.off_G = L.off_G;
+    a.off_Gi = L.off_Gi;
+    a.off_LU = L.off_LU;
+    a.off_v = L.off_v;
+    a.off_d = L.off_d;
+    a.off_perm = L.off_perm;
+    a.warp_bytes = L.bytes;
+}
+
+// Optional timing of the per-pixel kernel: CUDA events recorded on the launch
+// stream around each k_pixel launch while enabled (used by the benchmark).
+struct PixTimer {
+    std::mutex mu;
+    bool on = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+};
+static PixTimer g_timer;
+
+template <int MODE>
+static dpl_status launch_pixel(PixArgs& a, cudaStream_t s);
+
+template <int MODE>
+static dpl_status launch_pixel_timed(PixArgs& a, cudaStream_t s) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_timer.mu);
+        if (g_timer.on) {
+            DPL_CUDA_TRY(cudaEventCreate(&e0));
+            DPL_CUDA_TRY(cudaEventCreate(&e1));
+            g_timer.ev.emplace_back(e0, e1);
+        }
+    }
+    if (e0) DPL_CUDA_TRY(cudaEventRecord(e0, s));
+    dpl_status st = launch_pixel<MODE>(a, s);
+    if (e1) DPL_CUDA_TRY(cudaEventRecord(e1, s));
+    return st;
+}
+
+template <int MODE>
+static dpl_status launch_pixel(PixArgs& a, cudaStream_t s) {
+    if (a.npix == 0) return DPL_OK;
+    int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)(110 * 1024) / a.warp_bytes));
+    size_t smem = (size_t)warps * a.warp_bytes;
+    if (smem > 220 * 1024) return fail(DPL_ERR_UNSUPPORTED, "per-pixel shared memory exceeds the SM limit");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto go = [&](auto kernel) -> dpl_status {
+        DPL_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, warps * 32, smem));
+        int64_t want = (a.npix + warps - 1) / warps;
+        int64_t grid = std::min<int64_t>(want, (int64_t)std::max(1, per_sm) * std::max(1, sms) * 8);
+        kernel<<<(unsigned)grid, warps * 32, smem, s>>>(a);
+        return check_launch("k_pixel");
+    };
+    if (a.n <= 32) return go(k_pixel<1, MODE>);
+    return go(k_pixel<2, MODE>);
+}
+
+static int norm_ref(int ref, int n) { return ref < 0 ? n + ref : ref; }
+
+static void set_solver_params(PixArgs& a, int use_evd, double beta, double zct, int ref_idx, double num_looks,
+                              int first_real, int compute_crlb) {
+    a.use_evd = use_evd;
+    a.beta_on = beta > 0.0;
+    a.one_minus_beta = (float)(1.0 - beta);
+    a.beta = (float)beta;
+    a.zct = (float)zct;
+    a.ref_idx = ref_idx;
+    a.compute_crlb = compute_crlb;
+    a.crlb_ref = std::max(first_real - 1, 0);
+    a.crlb_factor = (float)(2.0 * num_looks);
+}
+
+struct PlWorkspace {
+    int* status;
+    unsigned int* valid_bits;
+    uint8_t* flags;
+    float* avgmag;
+    cfloat* zt;
+    cfloat* V;
+    float* CR;
+};
+
+static size_t pl_workspace_layout(int64_t n, int64_t rows, int64_t cols, int sy, int sx, char* base, PlWorkspace* w) {
+    Workspace ws{base, ~size_t(0)};
+    const int64_t npix = rows * cols, P = (rows / sy) * (cols / sx);
+    PlWorkspace t{};
+    t.status = ws.take<int>(16);
+    t.valid_bits = ws.take<unsigned int>(16);
+    t.flags = ws.take<uint8_t>(npix);
+    t.avgmag = ws.take<float>(npix);
+    t.zt = ws.take<cfloat>(npix * n);
+    t.V = ws.take<cfloat>(P * n);
+    t.CR = ws.take<float>(P * n);
+    if (w) *w = t;
+    return align_up(ws.used, 256);
+}
+
+static dpl_status validate_common(int64_t n, int64_t rows, int64_t cols, int hy, int hx, int sy, int sx) {
+    if (n <= 0 || rows <= 0 || cols <= 0 || hy < 0 || hx < 0 || sy <= 0 || sx <= 0)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "bad shape or window");
+    if (n > kMaxNslc) return fail(DPL_ERR_UNSUPPORTED, "at most 64 SLCs per call are supported");
+    if (2 * hx + 1 > 64) return fail(DPL_ERR_UNSUPPORTED, "window width 2*hx+1 must be <= 64");
+    if (rows > INT32_MAX / 2 || cols > INT32_MAX / 2) return fail(DPL_ERR_UNSUPPORTED, "image too large");
+    if (2 * hy + 1 > rows || 2 * hx + 1 > cols)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "half_window is larger than the SLC stack");
+    return DPL_OK;
+}
+
+}  // namespace dpl
+
+using namespace dpl;
+
+extern "C" size_t dpl_phase_link_workspace_size(const dpl_pl_params* p) {
+    if (!p) return 0;
+    return pl_workspace_layout(p->nslc, p->rows, p->cols, std::max(1, p->sy), std::max(1, p->sx), nullptr, nullptr);
+}
+
+extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
+                                     void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
+    if (!prm || !in || !out) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link: null argument");
+    const dpl_pl_params& P = *prm;
+    dpl_status st = validate_common(P.nslc, P.rows, P.cols, P.hy, P.hx, P.sy, P.sx);
+    if (st != DPL_OK) return st;
+    if (!in->slc || !out->cpx_phase || !out->temp_coh || !out->eigenvalues || !out->estimator || !out->crlb_std_dev)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link: null array");
+    const int n = (int)P.nslc;
+    const int ref = norm_ref(P.reference_idx, n);
+    if (ref < 0 || ref >= n) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
+    if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    PlWorkspace w;
+    pl_workspace_layout(P.nslc, P.rows, P.cols, P.sy, P.sx, (char*)workspace, &w);
+    const int64_t npix = P.rows * P.cols;
+    const int out_rows = (int)(P.rows / P.sy), out_cols = (int)(P.cols / P.sx);
+    const int64_t Pout = (int64_t)out_rows * out_cols;
+    DPL_CUDA_TRY(cudaMemsetAsync(w.status, 0, 64, s));
+    DPL_CUDA_TRY(cudaMemsetAsync(w.valid_bits, 0, 64, s));
+    {
+        size_t smem = (size_t)kPrepPix * (n + 1) * sizeof(cfloat);
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_prep<<<ceil_div(npix, kPrepPix), 256, smem, s>>>(
+            reinterpret_cast<const cfloat*>(in->slc), n, npix, in->nodata_mask, in->ps_mask, P.mask_input_ps, w.flags,
+            w.zt, in->avg_mag ? nullptr : w.avgmag, w.valid_bits);
+        st = check_launch("k_prep");
+        if (st != DPL_OK) return st;
+    }
+    if (Pout > 0) {
+        PixArgs a{};
+        fill_pix_layout(a, n, 2 * P.hx + 1);
+        a.rows = (int)P.rows;
+        a.cols = (int)P.cols;
+        a.hy = P.hy;
+        a.hx = P.hx;
+        a.sy = P.sy;
+        a.sx = P.sx;
+        a.out_rows = out_rows;
+        a.out_cols = out_cols;
+        a.npix = Pout;
+        a.zt = w.zt;
+        a.nb_u8 = in->neighbors;
+        set_solver_params(a, P.use_evd, P.beta, P.zero_correlation_threshold, ref, std::sqrt((double)P.hy * P.hx),
+                          P.first_real_slc_idx, P.compute_crlb);
+        a.baseline_lag = P.baseline_lag > 0 ? P.baseline_lag : 0;
+        a.vout = w.V;
+        a.eig = out->eigenvalues;
+        a.est = out->estimator;
+        a.crlb = w.CR;
+        a.tcoh = out->temp_coh;
+        a.closure = n > 2 ? out->closure_phases : nullptr;
+        a.counts = in->neighbors ? out->shp_counts : nullptr;
+        st = launch_pixel_timed<kFused>(a, s);
+        if (st != DPL_OK) return st;
+
+        PostArgs q{};
+        q.n = n;
+        q.rows = (int)P.rows;
+        q.cols = (int)P.cols;
+        q.sy = P.sy;
+        q.sx = P.sx;
+        q.out_rows = out_rows;
+        q.out_cols = out_cols;
+        q.slc = reinterpret_cast<const cfloat*>(in->slc);
+        q.flags = w.flags;
+        q.mag = in->avg_mag ? in->avg_mag : w.avgmag;
+        q.V = w.V;
+        q.CR = w.CR;
+        q.use_max_ps = P.use_max_ps;
+        q.use_slc_amp = P.use_slc_amp;
+        q.ref_idx = ref;
+        q.cpx = reinterpret_cast<cfloat*>(out->cpx_phase);
+        q.tcoh = out->temp_coh;
+        q.crlb = out->crlb_std_dev;
+        q.status = w.status;
+        k_post<<<ceil_div(Pout, 256), 256, 0, s>>>(q);
+        st = check_launch("k_post");
+        if (st != DPL_OK) return st;
+    }
+    int host_status[2] = {0, 0};
+    unsigned int host_valid[2] = {0, 0};
+    DPL_CUDA_TRY(cudaMemcpyAsync(host_status, w.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DPL_CUDA_TRY(cudaMemcpyAsync(host_valid, w.valid_bits, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    DPL_CUDA_TRY(cudaStreamSynchronize(s));
+    const unsigned long long vb = host_valid[0] | ((unsigned long long)host_valid[1] << 32);
+    std::vector<int> bad;
+    for (int t = 0; t < n; ++t)
+        if (!((vb >> t) & 1ull)) bad.push_back(t);
+    if (!bad.empty()) {
+        std::ostringstream os;
+        os << "slc_stack[[";
+        for (size_t i = 0; i < bad.size(); ++i) os << (i ? " " : "") << bad[i];
+        os << "]] out of " << n << " are all NaNs.";
+        return fail(DPL_ERR_ALL_NAN_SLC, os.str());
+    }
+    if (host_status[0] == DPL_ERR_INVALID_ARGUMENT)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "a PS look window has no finite brightness (avg_mag is NaN at its PS pixels)");
+    if (host_status[0] != 0) return fail((dpl_status)host_status[0], "device-side error");
+    return DPL_OK;
+}
+
+extern "C" size_t dpl_covariance_workspace_size(int64_t nslc, int64_t rows, int64_t cols) {
+    Workspace ws{nullptr, ~size_t(0)};
+    ws.take<int>(16);
+    ws.take<unsigned int>(16);
+    ws.take<uint8_t>(rows * cols);
+    ws.take<cfloat>(rows * cols * nslc);
+    return align_up(ws.used, 256);
+}
+
+extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t rows, int64_t cols, int hy, int hx,
+                                     int sy, int sx, const uint8_t* neighbors, float* C, void* workspace,
+                                     size_t workspace_bytes, dpl_stream_t stream) {
+    dpl_status st = validate_common(nslc, rows, cols, hy, hx, sy, sx);
+    if (st != DPL_OK) return st;
+    if (!slc || !C || !workspace) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: null pointer");
+    if (workspace_bytes < dpl_covariance_workspace_size(nslc, rows, cols))
+        return fail(DPL_ERR_WORKSPACE, "dpl_covariance: workspace too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = (int)nslc;
+    Workspace ws{(char*)workspace, workspace_bytes};
+    int* status = ws.take<int>(16);
+    unsigned int* vb = ws.take<unsigned int>(16);
+    uint8_t* flags = ws.take<uint8_t>(rows * cols);
+    cfloat* zt = ws.take<cfloat>(rows * cols * nslc);
+    (void)status;
+    const int64_t npix = rows * cols;
+    size_t smem = (size_t)kPrepPix * (n + 1) * sizeof(cfloat);
+    DPL_CUDA_TRY(cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_prep<<<ceil_div(npix, kPrepPix), 256, smem, s>>>(reinterpret_cast<const cfloat*>(slc), n, npix, nullptr, nullptr,
+                                                       0, flags, zt, nullptr, vb);
+    st = check_launch("k_prep");
+    if (st != DPL_OK) return st;
+    PixArgs a{};
+    fill_pix_layout(a, n, 2 * hx + 1);
+    a.rows = (int)rows;
+    a.cols = (int)cols;
+    a.hy = hy;
+    a.hx = hx;
+    a.sy = sy;
+    a.sx = sx;
+    a.out_rows = (int)(rows / sy);
+    a.out_cols = (int)(cols / sx);
+    a.npix = (int64_t)a.out_rows * a.out_cols;
+    a.zt = zt;
+    a.nb_u8 = neighbors;
+    a.Cout = reinterpret_cast<cfloat*>(C);
+    return launch_pixel<kCovOnly>(a, s);
+}
+
+extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use_evd, double beta,
+                                            double zero_correlation_threshold, int reference_idx, double num_looks,
+                                            int first_real_slc_idx, int compute_crlb, float* eig_vecs,
+                                            float* eig_vals, uint8_t* estimator, float* crlb_std_dev,
+                                            float* temp_coh, float* closure_phases, dpl_stream_t stream) {
+    if (npix < 0 || nslc <= 0) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence: bad shape");
+    if (nslc > kMaxNslc) return fail(DPL_ERR_UNSUPPORTED, "at most 64 SLCs per call are supported");
+    if (npix == 0) return DPL_OK;
+    if (!C || !eig_vecs || !eig_vals || !estimator || !crlb_std_dev || !temp_coh)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence: null pointer");
+    const int ref = norm_ref(reference_idx, nslc);
+    if (ref < 0 || ref >= nslc) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
+    PixArgs a{};
+    fill_pix_layout(a, nslc, 1);
+    a.npix = npix;
+    a.Cin = reinterpret_cast<const cfloat*>(C);
+    set_solver_params(a, use_evd, beta, zero_correlation_threshold, ref, num_looks, first_real_slc_idx, compute_crlb);
+    a.vout = reinterpret_cast<cfloat*>(eig_vecs);
+    a.eig = eig_vals;
+    a.est = estimator;
+    a.crlb = crlb_std_dev;
+    a.tcoh = temp_coh;
+    a.closure = nslc > 2 ? closure_phases : nullptr;
+    return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream);
+}
+
+extern "C" dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches) {
+    std::lock_guard<std::mutex> g(g_timer.mu);
+    double tot = 0.0;
+    int64_t cnt = 0;
+    for (auto& pr : g_timer.ev) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(pr.second) == cudaSuccess && cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
+            tot += ms;
+            ++cnt;
+        }
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    g_timer.ev.clear();
+    g_timer.on = enable != 0;
+    if (total_ms) *total_ms = tot;
+    if (launches) *launches = cnt;
+    return DPL_OK;
+}

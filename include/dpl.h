@@ -1,0 +1,179 @@
+/*
+ * dpl.h -- C ABI of the GB300 phase-linking library (libdpl.so).
+ *
+ * Every entry point takes DEVICE pointers, sizes, parameters and a CUDA stream,
+ * enqueues its kernels on that stream and returns without synchronising (except
+ * where noted).  No entry point allocates device memory: scratch space is passed
+ * in by the caller (`workspace`, sized by the matching *_workspace_size call).
+ * Arrays are C-contiguous; complex values are interleaved float pairs
+ * (numpy complex64 layout); boolean arrays are one byte per element (0/1).
+ *
+ * Each function names the reference (dolphin) interface it replaces; paths are
+ * relative to the dolphin source tree (src/dolphin/...).
+ */
+#ifndef DPL_H_
+#define DPL_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A cudaStream_t (the CUDA runtime and driver handle types are the same pointer). */
+typedef struct CUstream_st* dpl_stream_t;
+
+typedef enum dpl_status {
+    DPL_OK = 0,
+    DPL_ERR_INVALID_ARGUMENT = 1, /* maps to ValueError */
+    DPL_ERR_ALL_NAN_SLC = 2,      /* maps to PhaseLinkRuntimeError (phase_link/_core.py:564-571) */
+    DPL_ERR_CUDA = 3,             /* a CUDA call failed; maps to RuntimeError */
+    DPL_ERR_WORKSPACE = 4,        /* workspace smaller than *_workspace_size() */
+    DPL_ERR_UNSUPPORTED = 5,      /* parameters outside the supported range (e.g. nslc > 64) */
+    DPL_ERR_TIMEOUT = 6           /* a bounded device-side wait gave up; no result written */
+} dpl_status;
+
+/* Message for the last non-OK status returned on the calling host thread. */
+const char* dpl_last_error_message(void);
+
+/* Library ABI version (major * 1000 + minor). */
+int dpl_version(void);
+
+/* Largest number of SLCs a phase-linking call accepts. */
+int dpl_max_nslc(void);
+
+/* ---------------------------------------------------------------------------------
+ * Amplitude dispersion / PS selection.
+ * Replaces: calc_ps_block(stack_mag, amp_dispersion_threshold, min_count)  -- ps.py:169-244
+ *
+ * stack_mag : (nslc, npix) float32, may hold NaN
+ * mean      : (npix) float32 out  -- nanmean, NaN/inf -> 0
+ * amp_disp  : (npix) float32 out  -- nanstd/nanmean, 0 where count < min_count
+ * ps        : (npix) uint8 out    -- amp_disp < threshold and amp_disp != 0
+ * The comparison is done in float32 against `threshold` (numpy's rule for a Python
+ * float threshold); pass threshold_is_f64=1 to compare in float64 against
+ * `threshold64` (numpy's rule for a numpy float64 threshold).
+ * ------------------------------------------------------------------------------- */
+dpl_status dpl_ps_block(const float* stack_mag, int64_t nslc, int64_t npix, float threshold,
+                        int threshold_is_f64, double threshold64, int64_t min_count,
+                        float* mean, float* amp_disp, uint8_t* ps, dpl_stream_t stream);
+
+/* ---------------------------------------------------------------------------------
+ * SHP selection by the GLRT on Rayleigh scale parameters.
+ * Replaces: shp._glrt.estimate_neighbors(mean, var, halfwin_rowcol, strides, nslc, alpha)
+ *           -- shp/_glrt.py:13-130 (dispatched from shp/__init__.py:83-99)
+ *
+ * mean, var : (rows, cols) float32
+ * threshold : chi2.ppf(1 - alpha, df=1), rounded to float32 by the caller
+ * is_shp    : (rows / sy, cols / sx, 2*hy+1, 2*hx+1) uint8 out
+ * workspace : dpl_shp_glrt_workspace_size(rows, cols) bytes
+ * ------------------------------------------------------------------------------- */
+size_t dpl_shp_glrt_workspace_size(int64_t rows, int64_t cols);
+dpl_status dpl_shp_glrt(const float* mean, const float* var, int64_t rows, int64_t cols, int hy,
+                        int hx, int sy, int sx, int nslc, float threshold, uint8_t* is_shp,
+                        void* workspace, size_t workspace_bytes, dpl_stream_t stream);
+
+/* ---------------------------------------------------------------------------------
+ * SHP selection by the two-sample Kolmogorov-Smirnov test.
+ * Replaces: shp._ks.estimate_neighbors(amp_stack, halfwin_rowcol, alpha, strides, is_sorted)
+ *           -- shp/_ks.py:22-98 with _set_neighbors / _get_max_cdf_dist (:139-218)
+ *
+ * amp_stack : (nslc, rows, cols) float32 (sorted along axis 0 if is_sorted)
+ * cutoff    : critical ECDF distance (shp/_ks.py:221-239), float64
+ * is_shp    : (rows / sy, cols / sx, 2*hy+1, 2*hx+1) uint8 out
+ * workspace : dpl_shp_ks_workspace_size(nslc, rows, cols) bytes
+ * ------------------------------------------------------------------------------- */
+size_t dpl_shp_ks_workspace_size(int64_t nslc, int64_t rows, int64_t cols);
+dpl_status dpl_shp_ks(const float* amp_stack, int64_t nslc, int64_t rows, int64_t cols, int hy,
+                      int hx, int sy, int sx, double cutoff, int is_sorted, uint8_t* is_shp,
+                      void* workspace, size_t workspace_bytes, dpl_stream_t stream);
+
+/* ---------------------------------------------------------------------------------
+ * Phase linking.
+ * Replaces: phase_link.run_phase_linking(...)  -- phase_link/_core.py:67-249
+ *           (run_cpl :252-376, process_coherence_matrices :379-534)
+ * ------------------------------------------------------------------------------- */
+typedef struct dpl_pl_params {
+    int64_t nslc, rows, cols;      /* slc_stack shape */
+    int hy, hx;                    /* half_window (y, x) */
+    int sy, sx;                    /* strides (y, x) */
+    int use_evd;                   /* 1: EVD for every pixel */
+    double beta;                   /* |Gamma| regularisation (Python float; rounded like jax) */
+    double zero_correlation_threshold;
+    int reference_idx;             /* negative counts from the end */
+    int mask_input_ps;
+    int use_max_ps;
+    int use_slc_amp;
+    int baseline_lag;              /* <= 0: off */
+    int first_real_slc_idx;
+    int compute_crlb;
+} dpl_pl_params;
+
+typedef struct dpl_pl_inputs {
+    const float* slc;              /* (nslc, rows, cols) complex64 */
+    const uint8_t* nodata_mask;    /* (rows, cols) or NULL */
+    const uint8_t* ps_mask;        /* (rows, cols) or NULL */
+    const uint8_t* neighbors;      /* (out_rows, out_cols, 2hy+1, 2hx+1) or NULL (rectangular window) */
+    const float* avg_mag;          /* (rows, cols) or NULL (nanmean |slc| is used) */
+} dpl_pl_inputs;
+
+typedef struct dpl_pl_outputs {
+    float* cpx_phase;              /* (nslc, out_rows, out_cols) complex64 */
+    float* temp_coh;               /* (out_rows, out_cols) float32 */
+    int32_t* shp_counts;           /* (out_rows, out_cols) int32; may be NULL when neighbors is NULL */
+    float* eigenvalues;            /* (out_rows, out_cols) float32 */
+    uint8_t* estimator;            /* (out_rows, out_cols) uint8: 0 EVD, 1 EMI */
+    float* crlb_std_dev;           /* (nslc, out_rows, out_cols) float32 */
+    float* closure_phases;         /* (out_rows, out_cols, nslc - 2) float32; may be NULL */
+} dpl_pl_outputs;
+
+size_t dpl_phase_link_workspace_size(const dpl_pl_params* params);
+
+/* Enqueues the whole pipeline, then synchronises the stream once to report an
+ * all-NaN SLC (DPL_ERR_ALL_NAN_SLC, with the reference's message) or a PS window
+ * whose brightness is undefined (DPL_ERR_INVALID_ARGUMENT). */
+dpl_status dpl_phase_link(const dpl_pl_params* params, const dpl_pl_inputs* inputs,
+                          const dpl_pl_outputs* outputs, void* workspace,
+                          size_t workspace_bytes, dpl_stream_t stream);
+
+/* ---------------------------------------------------------------------------------
+ * Stage entry points (used to check each stage against the oracle).
+ * ------------------------------------------------------------------------------- */
+
+/* Replaces: covariance.estimate_stack_covariance(slc_stack, half_window, strides,
+ *           neighbor_arrays) -- phase_link/covariance.py:24-107.
+ * C : (out_rows, out_cols, nslc, nslc) complex64 out.  NaN samples are masked. */
+size_t dpl_covariance_workspace_size(int64_t nslc, int64_t rows, int64_t cols);
+dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t rows, int64_t cols, int hy,
+                          int hx, int sy, int sx, const uint8_t* neighbors, float* C,
+                          void* workspace, size_t workspace_bytes, dpl_stream_t stream);
+
+/* Replaces: _core.process_coherence_matrices(C_arrays, ...) -- phase_link/_core.py:379-534,
+ *           followed by metrics.estimate_temp_coh (metrics.py:10-40) and
+ *           compute_nearest_closure_phases_batch (_closure_phase.py:23-40).
+ * C            : (npix, nslc, nslc) complex64 (baseline_lag, if any, already applied)
+ * eig_vecs     : (npix, nslc) complex64 out, referenced to reference_idx
+ * eig_vals     : (npix) float32;  estimator : (npix) uint8
+ * crlb_std_dev : (npix, nslc) float32 (zeros if !compute_crlb)
+ * temp_coh     : (npix) float32;  closure_phases : (npix, nslc - 2) float32 or NULL
+ * num_looks    : sqrt(hy * hx) in the reference */
+dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use_evd, double beta,
+                                 double zero_correlation_threshold, int reference_idx,
+                                 double num_looks, int first_real_slc_idx, int compute_crlb,
+                                 float* eig_vecs, float* eig_vals, uint8_t* estimator,
+                                 float* crlb_std_dev, float* temp_coh, float* closure_phases,
+                                 dpl_stream_t stream);
+
+/* Timing of the per-pixel phase-linking kernel (no reference counterpart: a
+ * measurement hook).  While enabled, dpl_phase_link records a CUDA event pair on
+ * its stream around each launch of that kernel.  Each call returns (and clears)
+ * the summed elapsed milliseconds and launch count of the pairs recorded since the
+ * previous call, waiting for them to complete, then sets the enable state. */
+dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DPL_H_ */

@@ -4,8 +4,10 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-if str(ROOT) not in sys.path:
-    sys.path.insert(0, str(ROOT))
+TESTS = Path(__file__).resolve().parent
+for _p in (ROOT, TESTS):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 

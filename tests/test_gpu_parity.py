@@ -1,0 +1,371 @@
+"""GPU parity: each CUDA stage through the C ABI against the golden vectors and the oracle.
+
+Masks (PS, GLRT, KS) must be bit-exact; phases within 1e-3 rad and temporal
+coherence within 1e-4 on pixels with coherence > 0.3 (the benchmark spec's tolerances).
+"""
+
+import ast
+
+import numpy as np
+import pytest
+
+from oracle import phase_link as O
+from parity import compare_pl, phase_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover - CPU container
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import dolphin_gb300 as dp  # noqa: E402
+from dolphin_gb300.simulate import StackConfig, make_stack  # noqa: E402
+
+PHASE_TOL = 1e-3  # rad
+TC_TOL = 1e-4
+
+
+# ---------------------------------------------------------------------------------
+# PS selection
+# ---------------------------------------------------------------------------------
+def test_ps_block_golden(golden):
+    g = golden("ps_block")
+    mag = g["mag"]
+    for k, (thr, mc) in enumerate(zip(g["thr"], g["min_count"])):
+        mean, disp, ps = dp.calc_ps_block(mag, float(thr), None if mc < 0 else int(mc))
+        assert mean.dtype == disp.dtype == np.float32 and ps.dtype == bool
+        np.testing.assert_array_equal(mean, g[f"mean_{k}"])
+        np.testing.assert_array_equal(disp, g[f"disp_{k}"])
+        np.testing.assert_array_equal(ps, g[f"ps_{k}"])
+
+
+@pytest.mark.parametrize("n", [1, 5, 30, 45, 70])
+def test_ps_block_bit_exact_random(n):
+    rng = np.random.default_rng(n)
+    mag = rng.lognormal(0, 0.6, size=(n, 37, 53)).astype(np.float32)
+    mag[rng.random(mag.shape) < 0.02] = np.nan
+    mag[:, 3, 4] = np.nan
+    mag[:, 5, 6] = 2.5
+    for thr, mc in ((0.25, None), (0.5, n), (np.float64(0.3), 1)):
+        got = dp.calc_ps_block(mag, thr, mc)
+        want = O.calc_ps_block(mag.copy(), thr, mc)
+        for a, b in zip(got, want):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_ps_block_rejects_complex():
+    with pytest.raises(ValueError):
+        dp.calc_ps_block(np.ones((3, 2, 2), np.complex64))
+
+
+def test_ps_block_empty_and_device_roundtrip():
+    mean, disp, ps = dp.calc_ps_block(np.zeros((4, 0, 3), np.float32))
+    assert mean.shape == (0, 3)
+    mag = torch.rand(6, 8, 9, device="cuda")
+    m, d, p = dp.calc_ps_block(mag)
+    assert m.is_cuda and p.dtype == torch.uint8
+    ref = O.calc_ps_block(mag.cpu().numpy())
+    np.testing.assert_array_equal(m.cpu().numpy(), ref[0])
+
+
+# ---------------------------------------------------------------------------------
+# SHP
+# ---------------------------------------------------------------------------------
+def test_glrt_golden(golden):
+    g = golden("glrt")
+    for k in range(int(g["ncases"])):
+        hy, hx, sy, sx, nslc, alpha = g[f"params_{k}"]
+        nb = dp.estimate_neighbors(halfwin_rowcol=(int(hy), int(hx)), strides=(int(sy), int(sx)),
+                                   mean=g[f"mean_{k}"], var=g[f"var_{k}"], nslc=int(nslc), alpha=alpha)
+        np.testing.assert_array_equal(nb, g[f"nb_{k}"])
+
+
+@pytest.mark.parametrize("hw,strides", [((5, 5), (1, 1)), ((5, 11), (1, 1)), ((3, 7), (2, 3)), ((7, 7), (4, 1)),
+                                        ((0, 0), (1, 1)), ((10, 31), (1, 2))])
+def test_glrt_vs_oracle(hw, strides):
+    rng = np.random.default_rng(17)
+    amp = rng.rayleigh(10.0, size=(20, 67, 141)).astype(np.float32)
+    amp[:, 10:30, 40:90] *= 2.5
+    mean, var = amp.mean(0), amp.var(0)
+    mean[:2, :3] = 0
+    var[5, 7] = np.nan
+    nb = dp.estimate_neighbors(halfwin_rowcol=hw, strides=strides, mean=mean, var=var, nslc=20, alpha=0.001)
+    ref, stat, thr = O.estimate_neighbors_glrt(mean, var, hw, strides, 20, 0.001, return_stat=True)
+    diff = nb != ref
+    # only pixels whose statistic is within float32 rounding of the cutoff may differ
+    near = np.abs(stat - thr) <= 1e-5 * thr
+    assert not (diff & ~near).any(), np.argwhere(diff & ~near)[:5]
+
+
+def test_glrt_window_larger_than_image():
+    with pytest.raises(ValueError):
+        dp.estimate_neighbors(halfwin_rowcol=(5, 5), mean=np.ones((4, 20), np.float32),
+                              var=np.ones((4, 20), np.float32), nslc=3, alpha=0.01)
+
+
+def test_glrt_requires_nslc():
+    with pytest.raises(ValueError):
+        dp.estimate_neighbors(halfwin_rowcol=(1, 1), mean=np.ones((4, 4)), var=np.ones((4, 4)), alpha=0.01)
+
+
+def test_shp_rect_and_unknown():
+    assert dp.estimate_neighbors(halfwin_rowcol=(1, 1), alpha=0.1, method="rect") is None
+    with pytest.raises(ValueError):
+        dp.estimate_neighbors(halfwin_rowcol=(1, 1), alpha=0.1, method="nope", nslc=3,
+                              mean=np.ones((4, 4)), var=np.ones((4, 4)))
+
+
+def test_ks_golden(golden):
+    g = golden("ks")
+    for k in range(int(g["ncases"])):
+        hy, hx, sy, sx, alpha = g[f"params_{k}"]
+        nb = dp.estimate_neighbors(halfwin_rowcol=(int(hy), int(hx)), strides=(int(sy), int(sx)),
+                                   amp_stack=g[f"amp_{k}"], alpha=alpha, method="ks")
+        np.testing.assert_array_equal(nb, g[f"nb_{k}"])
+
+
+@pytest.mark.parametrize("n", [7, 30, 64])
+def test_ks_vs_oracle(n):
+    rng = np.random.default_rng(n)
+    amp = rng.rayleigh(5.0, size=(n, 23, 29)).astype(np.float32)
+    amp[:, :8] *= 1.7
+    amp[:, 12, 12] = amp[:, 12, 13]  # exact ties
+    nb = dp.estimate_neighbors(halfwin_rowcol=(2, 3), amp_stack=amp, alpha=0.05, method="ks")
+    ref = O.estimate_neighbors_ks(amp, (2, 3), (1, 1), 0.05)
+    np.testing.assert_array_equal(nb, ref)
+    srt = np.sort(amp, axis=0)
+    nb2 = dp.estimate_neighbors(halfwin_rowcol=(2, 3), amp_stack=srt, alpha=0.05, method="ks", is_sorted=True)
+    np.testing.assert_array_equal(nb2, ref)
+
+
+def test_ks_requires_amp_stack():
+    with pytest.raises(ValueError):
+        dp.estimate_neighbors(halfwin_rowcol=(1, 1), alpha=0.1, method="ks")
+
+
+# ---------------------------------------------------------------------------------
+# covariance
+# ---------------------------------------------------------------------------------
+def test_covariance_golden(golden):
+    g = golden("covariance")
+    z = g["slc"]
+    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (1, 1)), g["C_rect"], atol=2e-6)
+    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (1, 1), g["nb"]), g["C_nb"], atol=2e-6)
+    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (2, 3)), g["C_strided"], atol=2e-6)
+
+
+@pytest.mark.parametrize("n", [3, 20, 33, 64])
+def test_covariance_vs_float64(n):
+    z = make_stack(StackConfig(nslc=n, rows=19, cols=27, seed=n, ps_frac=0.0))
+    z[1, 4, 5] = np.nan
+    got = dp.estimate_stack_covariance(z, (2, 3), (1, 2))
+    ref = O.estimate_stack_covariance(z.astype(np.complex128), (2, 3), (1, 2), dtype=np.float64)
+    np.testing.assert_allclose(got, ref, atol=5e-6)
+
+
+def test_covariance_rejects_real():
+    with pytest.raises(ValueError, match="complex"):
+        dp.estimate_stack_covariance(np.ones((3, 5, 5), np.float32), (1, 1))
+
+
+# ---------------------------------------------------------------------------------
+# eigen-solvers (process_coherence_matrices), tests modelled on the reference's
+# eigen tests: simulated coherence matrices, compared with numpy eigh
+# ---------------------------------------------------------------------------------
+def _sim_C(n, seed, rows=6, cols=7):
+    rng = np.random.default_rng(seed)
+    gamma = (0.99 - 0.95) * np.exp(-np.abs(np.subtract.outer(np.arange(n), np.arange(n))) * 12 / 72) + 0.95
+    np.fill_diagonal(gamma, 1.0)
+    out = np.empty((rows, cols, n, n), np.complex64)
+    for r in range(rows):
+        for c in range(cols):
+            ph = rng.normal(scale=0.5, size=n)
+            out[r, c] = gamma * np.exp(1j * np.subtract.outer(ph, ph))
+    return out
+
+
+def test_evd_matches_eigh():
+    C = _sim_C(20, 1)
+    vec, val, est, _ = dp.process_coherence_matrices(C, use_evd=True, compute_crlb=False)
+    w, v = np.linalg.eigh(C * np.abs(C))
+    np.testing.assert_allclose(val, w[..., -1], rtol=2e-5)
+    ref = v[..., -1] * np.exp(-1j * np.angle(v[..., :1, -1]))
+    assert phase_err(vec, ref).max() < 5e-3
+    assert (est == 0).all()
+
+
+def test_emi_matches_eigh():
+    C = _sim_C(20, 2)
+    vec, val, est, _ = dp.process_coherence_matrices(C, compute_crlb=False)
+    A = C * np.linalg.inv(np.abs(C).astype(np.float64) + 1e-6 * np.eye(20))
+    w, v = np.linalg.eigh(A)
+    np.testing.assert_allclose(val, w[..., 0], atol=2e-4)
+    ref = v[..., 0] * np.exp(-1j * np.angle(v[..., :1, 0]))
+    assert phase_err(vec, ref).max() < 1e-3
+    assert (est == 1).all()
+
+
+@pytest.mark.parametrize("n,kw", [
+    (10, dict()),
+    (30, dict(beta=0.1, zero_correlation_threshold=0.05, reference_idx=3, first_real_slc_idx=4)),
+    (45, dict(use_evd=True)),
+    (64, dict(reference_idx=-1)),
+])
+def test_process_coherence_vs_oracle(n, kw):
+    z = make_stack(StackConfig(nslc=n, rows=18, cols=20, seed=100 + n, ps_frac=0.0))
+    C = O.estimate_stack_covariance(z, (5, 5), (1, 1))
+    vec, val, est, crlb, tc, clos = dp.process_coherence_matrices(C, num_looks=5.0, return_metrics=True, **kw)
+    okw = dict(kw)
+    ref_idx = okw.pop("reference_idx", 0)
+    ref_idx = ref_idx + n if ref_idx < 0 else ref_idx
+    rv, rl, re_, rc = O.process_coherence_matrices(C.reshape(-1, n, n), num_looks=5.0, reference_idx=ref_idx, **okw)
+    rtc = O.estimate_temp_coh(rv, C.reshape(-1, n, n))
+    np.testing.assert_array_equal(est.ravel(), re_)
+    good = rtc > 0.3
+    assert phase_err(vec.reshape(-1, n)[good], rv[good]).max() < PHASE_TOL
+    np.testing.assert_allclose(np.abs(vec.reshape(-1, n)), np.abs(rv), rtol=1e-3, atol=1e-4)
+    np.testing.assert_allclose(val.ravel(), rl, rtol=1e-3)
+    assert np.abs(tc.ravel() - rtc)[good].max() < TC_TOL
+    np.testing.assert_allclose(crlb.reshape(-1, n), rc, rtol=3e-3, atol=1e-5)
+    rcl = O.closure_phases(C.reshape(-1, n, n))
+    assert phase_err(np.exp(1j * clos.reshape(rcl.shape)), np.exp(1j * rcl)).max() < 1e-5
+
+
+def test_singular_gamma_falls_back_to_evd():
+    # duplicate SLC -> rank-deficient C -> the Cholesky of |C| fails -> EVD, estimator 0
+    n = 8
+    C = np.ones((1, n, n), np.complex64) * 0.999
+    C[0][np.diag_indices(n)] = 1
+    C[0, :, 3] = C[0, :, 2]
+    C[0, 3, :] = C[0, 2, :]
+    vec, val, est, crlb = dp.process_coherence_matrices(C)
+    rv, rl, re_, rc = O.process_coherence_matrices(C)
+    np.testing.assert_array_equal(est, re_)
+    np.testing.assert_array_equal(np.isnan(crlb), np.isnan(rc))
+
+
+# ---------------------------------------------------------------------------------
+# run_phase_linking end to end
+# ---------------------------------------------------------------------------------
+def test_run_phase_linking_golden_cases(golden):
+    g = golden("phase_link")
+    specs = ast.literal_eval(str(g["specs"][0]))
+    for idx, (zname, hw, strides, kw) in specs.items():
+        kw = dict(kw)
+        for key in ("ps_mask", "nodata_mask", "neighbor_arrays", "avg_mag"):
+            if key in kw:
+                kw[key] = np.array(g[kw[key]])
+        out = dp.run_phase_linking(np.array(g[zname]), hw, strides, **kw)
+        compare_pl(out, g, idx)
+
+
+def test_config1_crop_golden(golden):
+    g = golden("config1_crop")
+    diag = {}
+    O.run_phase_linking(g["slc"], (5, 5), (1, 1), ps_mask=g["ps"].copy(), neighbor_arrays=g["nb"],
+                        avg_mag=g["mean"], diagnostics=diag)
+    out = dp.run_phase_linking(g["slc"], (5, 5), ps_mask=g["ps"], neighbor_arrays=g["nb"], avg_mag=g["mean"])
+    compare_pl(out, g, "emi", borderline=diag["gamma_min_eig"] < 1e-4)
+
+
+@pytest.mark.parametrize("strides", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("half_window", [5, 11])
+@pytest.mark.parametrize("shape", [(10, 11), (15, 20), (50, 75)])
+def test_strides_window_sizes(strides, half_window, shape):
+    """Mirror of the reference's smoke test over shapes, windows and strides."""
+    rng = np.random.default_rng(0)
+    data = rng.normal(0, 1, size=(4, *shape)).astype(np.complex64)
+    if 2 * half_window + 1 > shape[0]:
+        with pytest.raises(ValueError):
+            dp.run_phase_linking(data, dp.HalfWindow(half_window, half_window), dp.Strides(strides, strides))
+        return
+    out = dp.run_phase_linking(data, dp.HalfWindow(half_window, half_window), dp.Strides(strides, strides))
+    assert out.cpx_phase.shape == (4, shape[0] // strides, shape[1] // strides)
+
+
+def test_config1_full_vs_oracle_f32_and_f64():
+    """Config 1 (N=10, 128x128, hw 5x5, GLRT 0.001, EMI, PS 0.25) against both oracles."""
+    z = make_stack(StackConfig())
+    amp = np.abs(z)
+    mean, disp, ps = dp.calc_ps_block(amp, 0.25, 10)
+    var = (disp * mean) ** 2
+    nb = dp.estimate_neighbors(halfwin_rowcol=(5, 5), alpha=0.001, mean=mean, var=var, nslc=10)
+    out = dp.run_phase_linking(z, (5, 5), ps_mask=ps, neighbor_arrays=nb, avg_mag=mean)
+    diag = {}
+    ref = O.run_phase_linking(z, (5, 5), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, diagnostics=diag)
+    ref64 = O.run_phase_linking(z, (5, 5), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, dtype=np.float64)
+    border = diag["gamma_min_eig"] < 1e-4
+    np.testing.assert_array_equal(out.estimator[~border], ref.estimator[~border])
+    good = (ref.temp_coh > 0.3) & ~border & np.all(np.isfinite(ref.cpx_phase), axis=0)
+    assert good.mean() > 0.5
+    e32 = phase_err(out.cpx_phase[:, good], ref.cpx_phase[:, good]).max()
+    e64 = phase_err(out.cpx_phase[:, good], ref64.cpx_phase[:, good]).max()
+    assert e32 < PHASE_TOL, e32
+    assert e64 < PHASE_TOL, e64
+    assert np.abs(out.temp_coh[good] - ref.temp_coh[good]).max() < TC_TOL
+    assert np.abs(out.temp_coh[good] - ref64.temp_coh[good]).max() < TC_TOL
+
+
+def test_all_nan_slc_raises():
+    z = make_stack(StackConfig(nslc=5, rows=12, cols=12))
+    z[2] = np.nan
+    with pytest.raises(dp.PhaseLinkRuntimeError, match=r"slc_stack\[\[2\]\] out of 5 are all NaNs."):
+        dp.run_phase_linking(z, (2, 2))
+
+
+def test_mask_shape_and_dtype_errors():
+    z = make_stack(StackConfig(nslc=5, rows=12, cols=12))
+    with pytest.raises(ValueError, match="nodata_mask.shape"):
+        dp.run_phase_linking(z, (2, 2), nodata_mask=np.zeros((3, 3), bool))
+    with pytest.raises(ValueError, match="complex"):
+        dp.run_phase_linking(np.abs(z), (2, 2))
+
+
+def test_too_many_slcs_is_unsupported():
+    z = np.ones((65, 8, 8), np.complex64)
+    with pytest.raises(RuntimeError):
+        dp.run_phase_linking(z, (1, 1))
+
+
+def test_shift_nan_edges():
+    """Reference test_run_phase_linking_with_shift: NaN rows become nodata rows."""
+    z = make_stack(StackConfig(nslc=30, rows=11, cols=11, seed=3, ps_frac=0))
+    z[0, 0, :] = np.nan
+    z[1, -1, :] = np.nan
+    out = dp.run_phase_linking(z, (5, 5))
+    assert np.isnan(out.cpx_phase[:, [0, -1], :]).all()
+    assert np.isnan(out.temp_coh[[0, -1], :]).all()
+    assert np.all(~np.isnan(out.cpx_phase[:, 1:-1, :]))
+
+
+@pytest.mark.parametrize("use_max_ps", [True, False])
+@pytest.mark.parametrize("strides", [1, 2, 3])
+def test_ps_fill(use_max_ps, strides):
+    """Reference test_run_phase_linking_ps_fill: PS phase copied from the SLCs."""
+    z = make_stack(StackConfig(nslc=30, rows=11, cols=11, seed=4, ps_frac=0))
+    ps_mask = np.zeros((11, 11), bool)
+    ps_mask[2, 2] = True
+    out = dp.run_phase_linking(z, (5, 5), (strides, strides), ps_mask=ps_mask, use_max_ps=use_max_ps)
+    ps_phase = z[:, 2, 2] * np.conj(z[0, 2, 2])
+    o = 2 // strides
+    np.testing.assert_allclose(np.angle(out.cpx_phase[:, o, o] * np.conj(ps_phase)), 0, atol=1e-5)
+    assert out.temp_coh[o, o] == 1
+
+
+@pytest.mark.parametrize("use_slc_amp", [False, True])
+def test_use_slc_amp(use_slc_amp):
+    z = make_stack(StackConfig(nslc=30, rows=11, cols=11, seed=5, ps_frac=0))
+    ps_mask = np.zeros((11, 11), bool)
+    ps_mask[1, 1] = True
+    out = dp.run_phase_linking(z, (5, 5), ps_mask=ps_mask, use_slc_amp=use_slc_amp)
+    expected = np.abs(z) if use_slc_amp else 1
+    np.testing.assert_allclose(np.abs(out.cpx_phase), expected, rtol=1e-5)
+
+
+def test_device_tensors_stay_on_device():
+    z = make_stack(StackConfig(nslc=8, rows=16, cols=16))
+    zt = torch.from_numpy(z).cuda()
+    out = dp.run_phase_linking(zt, (2, 2))
+    assert out.cpx_phase.is_cuda and out.temp_coh.is_cuda
+    host = dp.run_phase_linking(z, (2, 2))
+    np.testing.assert_array_equal(out.cpx_phase.cpu().numpy(), host.cpx_phase)
