@@ -43,7 +43,8 @@ constexpr int kPrepPix = 64;
 __global__ void __launch_bounds__(256) k_prep(const cfloat* __restrict__ slc, int n, int64_t npix,
                                               const uint8_t* __restrict__ nodata_in,
                                               const uint8_t* __restrict__ ps_in, int mask_input_ps,
-                                              uint8_t* __restrict__ flags, cfloat* __restrict__ zt,
+                                              int nan_is_nodata, uint8_t* __restrict__ flags,
+                                              cfloat* __restrict__ zt,
                                               float* __restrict__ avgmag, unsigned int* __restrict__ valid_bits) {
     extern __shared__ cfloat prep_s[];  // [kPrepPix][n + 1]
     __shared__ uint8_t ign[kPrepPix];
@@ -76,7 +77,9 @@ __global__ void __launch_bounds__(256) k_prep(const cfloat* __restrict__ slc, in
                     ++mcnt;
                 }
             }
-            const bool nodata = (nodata_in && nodata_in[p]) || anynan;
+            // run_phase_linking marks a pixel with any NaN as nodata (_core.py:181);
+            // the bare covariance masks NaN samples one by one (covariance.py:122-123)
+            const bool nodata = (nodata_in && nodata_in[p]) || (nan_is_nodata && anynan);
             const bool ps = ps_in && ps_in[p] && !nodata;
             const bool ignore = nodata || (mask_input_ps && ps);
             flags[p] = (nodata ? kNodata : 0) | (ps ? kPs : 0) | (ignore ? kIgnore : 0);
@@ -921,7 +924,7 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
         size_t smem = (size_t)kPrepPix * (n + 1) * sizeof(cfloat);
         DPL_CUDA_TRY(cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_prep<<<ceil_div(npix, kPrepPix), 256, smem, s>>>(
-            reinterpret_cast<const cfloat*>(in->slc), n, npix, in->nodata_mask, in->ps_mask, P.mask_input_ps, w.flags,
+            reinterpret_cast<const cfloat*>(in->slc), n, npix, in->nodata_mask, in->ps_mask, P.mask_input_ps, 1, w.flags,
             w.zt, in->avg_mag ? nullptr : w.avgmag, w.valid_bits);
         st = check_launch("k_prep");
         if (st != DPL_OK) return st;
@@ -1028,7 +1031,7 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
     size_t smem = (size_t)kPrepPix * (n + 1) * sizeof(cfloat);
     DPL_CUDA_TRY(cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_prep<<<ceil_div(npix, kPrepPix), 256, smem, s>>>(reinterpret_cast<const cfloat*>(slc), n, npix, nullptr, nullptr,
-                                                       0, flags, zt, nullptr, vb);
+                                                       0, 0, flags, zt, nullptr, vb);
     st = check_launch("k_prep");
     if (st != DPL_OK) return st;
     PixArgs a{};
