@@ -64,7 +64,8 @@ SIGNATURES = {
     "dpl_phase_link": (_i, [C.POINTER(PlParams), C.POINTER(PlInputs), C.POINTER(PlOutputs), _p, _sz, _p]),
     "dpl_covariance_workspace_size": (_sz, [_i64, _i64, _i64]),
     "dpl_covariance": (_i, [_p, _i64, _i64, _i64, _i, _i, _i, _i, _p, _p, _p, _sz, _p]),
-    "dpl_process_coherence": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p]),
+    "dpl_process_coherence_workspace_size": (_sz, [_i64]),
+    "dpl_process_coherence": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _sz, _p]),
     "dpl_kernel_timing": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
 }
 

@@ -109,16 +109,17 @@ __global__ void __launch_bounds__(256) k_prep(const cfloat* __restrict__ slc, in
 // ---------------------------------------------------------------------------------
 // k_pixel: per-warp shared-memory layout
 // ---------------------------------------------------------------------------------
+// C (packed complex) | W1 (packed real) | S: staging for the window rows, or R (packed
+// complex) + W2 (packed real), or the full n x n LU of the fallback | v | d | piv
 struct PixLayout {
-    int n, ldm, ldg, np, stg;  // stg: staging length (complex) for one window row
-    size_t off_C, off_G, off_Gi, off_LU, off_v, off_d, off_perm, bytes;
+    int n, np, stg;
+    size_t off_C, off_W1, off_S, off_W2, off_v, off_d, off_piv, bytes;
 };
 
 inline PixLayout make_layout(int n, int wx) {
     PixLayout L{};
+    const size_t T = (size_t)n * (n + 1) / 2;
     L.n = n;
-    L.ldm = n | 1;
-    L.ldg = n | 1;
     L.np = (n + 1) & ~1;
     L.stg = wx * L.np + 32;
     size_t o = 0;
@@ -127,13 +128,15 @@ inline PixLayout make_layout(int n, int wx) {
         o = align_up(o + bytes, 16);
         return at;
     };
-    L.off_C = take((size_t)n * L.ldm * sizeof(cfloat));
-    L.off_G = take((size_t)n * L.ldg * sizeof(float));
-    L.off_Gi = take((size_t)n * L.ldg * sizeof(float));
-    L.off_LU = take(std::max((size_t)n * L.ldm, (size_t)L.stg) * sizeof(cfloat));
+    L.off_C = take(T * sizeof(cfloat));
+    L.off_W1 = take(T * sizeof(float));
+    const size_t rw2 = align_up(T * sizeof(cfloat), 16) + T * sizeof(float);
+    const size_t s_bytes = std::max({(size_t)L.stg * sizeof(cfloat), rw2, (size_t)n * n * sizeof(cfloat)});
+    L.off_S = take(s_bytes);
+    L.off_W2 = L.off_S + align_up(T * sizeof(cfloat), 16);
     L.off_v = take(64 * sizeof(cfloat));
     L.off_d = take(64 * sizeof(float));
-    L.off_perm = take(128 * sizeof(int));  // pivots [0, 64) and their permutation [64, 128)
+    L.off_piv = take(128 * sizeof(int));
     L.bytes = align_up(o, 128);
     return L;
 }
@@ -143,8 +146,8 @@ enum PixMode { kCovOnly = 0, kSolveOnly = 1, kFused = 2 };
 struct PixArgs {
     int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
     int64_t npix;
-    int ldm, ldg, np, stg;
-    size_t off_C, off_G, off_Gi, off_LU, off_v, off_d, off_perm, warp_bytes;
+    int np, stg;
+    size_t off_C, off_W1, off_S, off_W2, off_v, off_d, off_piv, warp_bytes;
     const cfloat* zt;        // (rows, cols, n) masked, pixel-major
     const uint8_t* nb_u8;    // (out_rows, out_cols, wy, wx) or null
     const uint32_t* nb_bits; // (out_rows, out_cols, wy, wpr) or null
@@ -164,18 +167,14 @@ struct PixArgs {
     int32_t* counts;         // (npix) or null
 };
 
-struct Mats {
-    cfloat* C;
-    float* G;
-    float* Gi;
-    cfloat* LU;
-    cfloat* v;
-    float* d;
-    int* perm;
-};
+}  // namespace dpl
+
+#include "solver.cuh"
+
+namespace dpl {
 
 // ---------------------------------------------------------------------------------
-// covariance (covariance.py:110-170): raw sums into C, then normalisation
+// covariance (covariance.py:110-170): raw sums into packed C, then normalisation
 // ---------------------------------------------------------------------------------
 __device__ __forceinline__ uint64_t row_mask(const PixArgs& a, int64_t p, int wa, int wx, int lane) {
     const uint64_t full = wx >= 64 ? ~0ull : ((1ull << wx) - 1ull);
@@ -195,12 +194,12 @@ __device__ __forceinline__ uint64_t row_mask(const PixArgs& a, int64_t p, int wa
 }
 
 template <int NB>
-__device__ void warp_covariance(const PixArgs& a, int64_t p, const Mats& m, int lane, int* count_out) {
+__device__ void warp_covariance(const PixArgs& a, int64_t p, cfloat* C, cfloat* stg, float* amp, int lane,
+                                int* count_out) {
     const int n = a.n, wy = 2 * a.hy + 1, wx = 2 * a.hx + 1, np = a.np;
     const int out_r = (int)(p / a.out_cols), out_c = (int)(p - (int64_t)out_r * a.out_cols);
     const int in_r = a.sy / 2 + out_r * a.sy, in_c = a.sx / 2 + out_c * a.sx;
     const int r0 = clamp_start_i(in_r, a.hy, wy, a.rows), c0 = clamp_start_i(in_c, a.hx, wx, a.cols);
-    cfloat* stg = m.LU;
     int count = 0;
     for (int rb = 0; rb < NB; ++rb) {
         for (int cb = rb; cb < NB; ++cb) {
@@ -212,6 +211,7 @@ __device__ void warp_covariance(const PixArgs& a, int64_t p, const Mats& m, int 
                 if (rb == 0 && cb == 0) count += __popcll(rm);
                 if (rm == 0ull) continue;
                 const cfloat* src = a.zt + ((int64_t)(r0 + wa) * a.cols + c0) * n;
+                __syncwarp();
                 for (int idx = lane; idx < a.stg; idx += 32) {
                     const int b = idx / np, t = idx - b * np;
                     stg[idx] = (b < wx && t < n) ? src[b * n + t] : cmake(0.f, 0.f);
@@ -231,421 +231,32 @@ __device__ void warp_covariance(const PixArgs& a, int64_t p, const Mats& m, int 
                         aim[2 * j2 + 1] += zi.im * q.z - zi.re * q.w;
                     }
                 }
-                __syncwarp();
             }
             const int row = rb * 32 + lane;
             if (row < n) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const int col = cb * 32 + j;
-                    if (col < n) {
-                        m.C[row * a.ldm + col] = cmake(are[j], aim[j]);
-                        if (rb != cb) m.C[col * a.ldm + row] = cmake(are[j], -aim[j]);
-                    }
+                    if (col <= row) C[pk(row, col)] = cmake(are[j], aim[j]);
+                    else if (rb != cb && col < n) C[pk(col, row)] = cmake(are[j], -aim[j]);
                 }
             }
-            __syncwarp();
         }
     }
-    // C = numer / sqrt(amp_i amp_j) where that root > 1e-6, else 0
-    for (int i = lane; i < n; i += 32) m.d[i] = m.C[i * a.ldm + i].re;
     __syncwarp();
-    for (int e = lane; e < n * n; e += 32) {
-        const int i = e / n, j = e - i * n;
-        const float s = fsqrt(fmul(m.d[i], m.d[j]));
-        cfloat c = m.C[i * a.ldm + j];
-        m.C[i * a.ldm + j] = s > 1e-6f ? cmake(fdiv(c.re, s), fdiv(c.im, s)) : cmake(0.f, 0.f);
+    // C = numer / sqrt(amp_i amp_j) where that root > 1e-6, else 0
+    for (int i = lane; i < n; i += 32) amp[i] = C[pk(i, i)].re;
+    __syncwarp();
+    for (int i = 0; i < n; ++i) {
+        const float ai = amp[i];
+        for (int j = lane; j <= i; j += 32) {
+            const float s = fsqrt(fmul(ai, amp[j]));
+            const cfloat c = C[pk(i, j)];
+            C[pk(i, j)] = s > 1e-6f ? cmake(fdiv(c.re, s), fdiv(c.im, s)) : cmake(0.f, 0.f);
+        }
     }
     __syncwarp();
     if (count_out) *count_out = count;
-}
-
-// ---------------------------------------------------------------------------------
-// dense per-warp linear algebra
-// ---------------------------------------------------------------------------------
-// Cholesky (lower, right-looking) in place; returns false on a non-positive pivot.
-__device__ bool warp_cholesky(float* G, int ldg, int n, int lane) {
-    for (int k = 0; k < n; ++k) {
-        const float dkk = G[k * ldg + k];
-        if (!(dkk > 0.f)) return false;  // uniform: every lane read the same value
-        const float lkk = fsqrt(dkk);
-        __syncwarp();
-        if (lane == 0) G[k * ldg + k] = lkk;
-        for (int i = k + 1 + lane; i < n; i += 32) G[i * ldg + k] = fdiv(G[i * ldg + k], lkk);
-        __syncwarp();
-        for (int i = k + 1 + lane; i < n; i += 32) {
-            const float lik = G[i * ldg + k];
-            for (int j = k + 1; j <= i; ++j) G[i * ldg + j] -= lik * G[j * ldg + k];
-        }
-        __syncwarp();
-    }
-    return true;
-}
-
-// Y = L^{-1} (lower) by column-parallel forward substitution.  If sumsq is non-null,
-// lane-owned columns also return sum_k Y[k][j]^2 (the diagonal of (L L^T)^{-1}).
-__device__ void warp_tri_inverse(const float* L, float* Y, int ldg, int n, int lane, float* sumsq) {
-    for (int j = lane; j < n; j += 32) {
-        const float yjj = fdiv(1.f, L[j * ldg + j]);
-        Y[j * ldg + j] = yjj;
-        float ss = yjj * yjj;
-        for (int i = j + 1; i < n; ++i) {
-            float s = 0.f;
-            for (int k = j; k < i; ++k) s += L[i * ldg + k] * Y[k * ldg + j];
-            const float yij = -fdiv(s, L[i * ldg + i]);
-            Y[i * ldg + j] = yij;
-            ss += yij * yij;
-        }
-        if (sumsq) sumsq[j] = ss;
-    }
-    __syncwarp();
-}
-
-// LU with partial pivoting (getrf: pivot = first maximum of |re| + |im|), in place.
-__device__ void warp_lu(cfloat* A, int ldm, int n, int* piv, int lane) {
-    for (int k = 0; k < n; ++k) {
-        float best = -1.f;
-        int bi = n;
-        for (int i = k + lane; i < n; i += 32) {
-            const cfloat x = A[i * ldm + k];
-            const float v = fabsf(x.re) + fabsf(x.im);
-            if (v > best) {
-                best = v;
-                bi = i;
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) {
-                best = ob;
-                bi = oi;
-            }
-        }
-        if (bi >= n) bi = k;
-        if (lane == 0) piv[k] = bi;
-        if (bi != k) {
-            for (int j = lane; j < n; j += 32) {
-                const cfloat t = A[k * ldm + j];
-                A[k * ldm + j] = A[bi * ldm + j];
-                A[bi * ldm + j] = t;
-            }
-        }
-        __syncwarp();
-        const cfloat pv = A[k * ldm + k];
-        if (pv.re != 0.f || pv.im != 0.f) {
-            const cfloat r = cdiv(cmake(1.f, 0.f), pv);
-            for (int i = k + 1 + lane; i < n; i += 32) A[i * ldm + k] = cmul(A[i * ldm + k], r);
-        }
-        __syncwarp();
-        for (int i = k + 1 + lane; i < n; i += 32) {
-            const cfloat lik = A[i * ldm + k];
-            for (int j = k + 1; j < n; ++j) A[i * ldm + j] = csub(A[i * ldm + j], cmul(lik, A[k * ldm + j]));
-        }
-        __syncwarp();
-    }
-}
-
-template <int NB>
-__device__ __forceinline__ cfloat bcast(const cfloat (&x)[NB], int k) {
-    cfloat r = shfl_c(x[0], k & 31);
-    if (NB > 1) {
-        cfloat r1 = shfl_c(x[NB - 1], k & 31);
-        if (k >= 32) r = r1;
-    }
-    return r;
-}
-
-template <int NB>
-__device__ __forceinline__ float vnorm2(const cfloat (&x)[NB]) {
-    float s = 0.f;
-#pragma unroll
-    for (int q = 0; q < NB; ++q) s += cabs2(x[q]);
-    return warp_sum(s);
-}
-
-// x <- (LU)^{-1} P x   (lu_solve: row interchanges, unit-lower then upper solve)
-template <int NB>
-__device__ void warp_lu_solve(const cfloat* A, int ldm, int n, const int* perm, cfloat (&x)[NB], int lane) {
-    cfloat w[NB];
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-        const int i = lane + 32 * q;
-        const int src = i < n ? perm[i] : 0;
-        cfloat t0 = shfl_c(x[0], src & 31);
-        cfloat t1 = NB > 1 ? shfl_c(x[NB - 1], src & 31) : t0;
-        w[q] = (i < n) ? ((src >= 32) ? t1 : t0) : cmake(0.f, 0.f);
-    }
-    for (int k = 0; k < n - 1; ++k) {
-        const cfloat xk = bcast<NB>(w, k);
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-            const int i = lane + 32 * q;
-            if (i > k && i < n) w[q] = csub(w[q], cmul(A[i * ldm + k], xk));
-        }
-    }
-    for (int k = n - 1; k >= 0; --k) {
-#pragma unroll
-        for (int q = 0; q < NB; ++q)
-            if (lane + 32 * q == k) w[q] = cdiv(w[q], A[k * ldm + k]);
-        const cfloat xk = bcast<NB>(w, k);
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-            const int i = lane + 32 * q;
-            if (i < k) w[q] = csub(w[q], cmul(A[i * ldm + k], xk));
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < NB; ++q) x[q] = w[q];
-}
-
-// y = M x with M[i][j] = B[i][j] (complex matrix in smem)
-template <int NB>
-__device__ void warp_matvec(const cfloat* B, int ldm, int n, const cfloat (&x)[NB], cfloat (&y)[NB], int lane) {
-#pragma unroll
-    for (int q = 0; q < NB; ++q) y[q] = cmake(0.f, 0.f);
-    for (int j = 0; j < n; ++j) {
-        const cfloat xj = bcast<NB>(x, j);
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-            const int i = lane + 32 * q;
-            if (i < n) y[q] = cadd(y[q], cmul(B[i * ldm + j], xj));
-        }
-    }
-}
-
-// Re(v^H A v) with A = Gi o C (real weights times complex entries)
-template <int NB>
-__device__ float warp_rayleigh_weighted(const float* W, int ldg, const cfloat* C, int ldm, int n,
-                                        const cfloat (&v)[NB], int lane) {
-    cfloat y[NB];
-#pragma unroll
-    for (int q = 0; q < NB; ++q) y[q] = cmake(0.f, 0.f);
-    for (int j = 0; j < n; ++j) {
-        const cfloat vj = bcast<NB>(v, j);
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-            const int i = lane + 32 * q;
-            if (i < n) y[q] = cadd(y[q], cmul(cscale(C[i * ldm + j], W[i * ldg + j]), vj));
-        }
-    }
-    float s = 0.f;
-#pragma unroll
-    for (int q = 0; q < NB; ++q) s += v[q].re * y[q].re + v[q].im * y[q].im;
-    return warp_sum(s);
-}
-
-template <int NB>
-__device__ float warp_rayleigh(const cfloat* B, int ldm, int n, const cfloat (&v)[NB], int lane) {
-    cfloat y[NB];
-    warp_matvec<NB>(B, ldm, n, v, y, lane);
-    float s = 0.f;
-#pragma unroll
-    for (int q = 0; q < NB; ++q) s += v[q].re * y[q].re + v[q].im * y[q].im;
-    return warp_sum(s);
-}
-
-// ---------------------------------------------------------------------------------
-// solver (process_coherence_matrices + temporal coherence + closure phases)
-// ---------------------------------------------------------------------------------
-__device__ __forceinline__ float gamma_reg(const PixArgs& a, const cfloat* C, int ldm, int i, int j) {
-    float g = cabs(C[i * ldm + j]);
-    if (a.beta_on) g = fadd(fmul(a.one_minus_beta, g), i == j ? a.beta : 0.f);
-    return g < a.zct ? 0.f : g;
-}
-
-template <int NB>
-__device__ void warp_solve(const PixArgs& a, int64_t p, const Mats& m, int lane) {
-    const int n = a.n, ldm = a.ldm, ldg = a.ldg;
-    cfloat* C = m.C;
-    if (a.baseline_lag > 0) {
-        for (int e = lane; e < n * n; e += 32) {
-            const int i = e / n, j = e - i * n;
-            if (abs(i - j) >= a.baseline_lag) C[i * ldm + j] = cmake(0.f, 0.f);
-        }
-        __syncwarp();
-    }
-    if (a.closure) {
-        for (int i = lane; i < n - 2; i += 32) {
-            const cfloat c = cmulc(cmul(C[i * ldm + i + 1], C[(i + 1) * ldm + i + 2]), C[i * ldm + i + 2]);
-            a.closure[p * (n - 2) + i] = atan2f(c.im, c.re);
-        }
-    }
-    // |Gamma| (+ regularisation) + 1e-6 I, Cholesky, inverse
-    float* G = m.G;
-    for (int e = lane; e < n * n; e += 32) {
-        const int i = e / n, j = e - i * n;
-        if (j <= i) G[i * ldg + j] = fadd(gamma_reg(a, C, ldm, i, j), i == j ? 1e-6f : 0.f);
-    }
-    __syncwarp();
-    const bool chol_ok = warp_cholesky(G, ldg, n, lane);
-    __syncwarp();
-    bool inv_nan;
-    if (chol_ok) {
-        warp_tri_inverse(G, m.Gi, ldg, n, lane, nullptr);
-        bool bad = false;
-        for (int e = lane; e < n * n; e += 32) {
-            const int i = e / n, j = e - i * n;
-            if (i <= j) {
-                float s = 0.f;
-                for (int k = j; k < n; ++k) s += m.Gi[k * ldg + i] * m.Gi[k * ldg + j];
-                G[i * ldg + j] = s;
-                G[j * ldg + i] = s;
-                bad |= isnan(s);
-            }
-        }
-        inv_nan = warp_any(bad);
-    } else {
-        for (int e = lane; e < n * n; e += 32) G[(e / n) * ldg + (e % n)] = nanf("");
-        inv_nan = true;
-    }
-    __syncwarp();
-
-    cfloat v[NB];
-    float lambda;
-    const bool evd = a.use_evd || inv_nan;
-    cfloat* LU = m.LU;
-    const float inv_sqrt_n = fdiv(1.f, fsqrt((float)n));
-#pragma unroll
-    for (int q = 0; q < NB; ++q) v[q] = (lane + 32 * q < n) ? cmake(inv_sqrt_n, 0.f) : cmake(0.f, 0.f);
-    if (!evd) {
-        // EMI: inverse iteration on (|Gamma|^-1 o C) - 0.99 I
-        for (int e = lane; e < n * n; e += 32) {
-            const int i = e / n, j = e - i * n;
-            cfloat x = cscale(C[i * ldm + j], G[i * ldg + j]);
-            if (i == j) x.re = fsub(x.re, 0.99f);
-            LU[i * ldm + j] = x;
-        }
-        __syncwarp();
-        warp_lu(LU, ldm, n, m.perm + 0, lane);
-        // permutation of the row interchanges (lane 0), stored after the pivots
-        int* perm = m.perm + 64;
-        if (lane == 0) {
-            for (int i = 0; i < n; ++i) perm[i] = i;
-            for (int k = 0; k < n; ++k) {
-                const int pk = m.perm[k];
-                const int t = perm[k];
-                perm[k] = perm[pk];
-                perm[pk] = t;
-            }
-        }
-        __syncwarp();
-        float diff = 1.f;
-        for (int it = 1; diff > 1e-5f && it < 50; ++it) {
-            cfloat x[NB];
-#pragma unroll
-            for (int q = 0; q < NB; ++q) x[q] = v[q];
-            warp_lu_solve<NB>(LU, ldm, n, perm, x, lane);
-            const float nrm = fsqrt(vnorm2<NB>(x));
-            float dd = 0.f;
-#pragma unroll
-            for (int q = 0; q < NB; ++q) {
-                x[q] = cmake(fdiv(x[q].re, nrm), fdiv(x[q].im, nrm));
-                dd += cabs2(csub(x[q], v[q]));
-                v[q] = x[q];
-            }
-            diff = fsqrt(warp_sum(dd));
-        }
-        lambda = warp_rayleigh_weighted<NB>(G, ldg, C, ldm, n, v, lane);
-        const float scale = fdiv(fsqrt((float)n), fsqrt(vnorm2<NB>(v)));
-#pragma unroll
-        for (int q = 0; q < NB; ++q) v[q] = cscale(v[q], scale);
-    } else {
-        // EVD: power iteration on C o |C|
-        for (int e = lane; e < n * n; e += 32) {
-            const int i = e / n, j = e - i * n;
-            const cfloat c = C[i * ldm + j];
-            LU[i * ldm + j] = cscale(c, cabs(c));
-        }
-        __syncwarp();
-        float diff = 1.f;
-        for (int it = 1; diff > 1e-5f && it < 50; ++it) {
-            cfloat y[NB];
-            warp_matvec<NB>(LU, ldm, n, v, y, lane);
-            const float nrm = fsqrt(vnorm2<NB>(y));
-            float dd = 0.f;
-#pragma unroll
-            for (int q = 0; q < NB; ++q) {
-                y[q] = cmake(fdiv(y[q].re, nrm), fdiv(y[q].im, nrm));
-                dd += cabs2(csub(y[q], v[q]));
-                v[q] = y[q];
-            }
-            diff = fsqrt(warp_sum(dd));
-        }
-        lambda = warp_rayleigh<NB>(LU, ldm, n, v, lane);
-    }
-    // reference to reference_idx: v * exp(-i angle(v[ref]))
-    const cfloat vr = bcast<NB>(v, a.ref_idx);
-    const cfloat rot = cconj(cphasor(vr));
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-        const int i = lane + 32 * q;
-        if (i < n) {
-            v[q] = cmul(v[q], rot);
-            m.v[i] = v[q];
-            a.vout[p * n + i] = v[q];
-        }
-    }
-    if (lane == 0) {
-        a.eig[p] = lambda;
-        a.est[p] = evd ? 0 : 1;
-    }
-    __syncwarp();
-    // temporal coherence over i < j (metrics.py:74-97, unit weights)
-    {
-        float sre = 0.f, sim = 0.f;
-        int cnt = 0;
-        for (int i = 0; i < n - 1; ++i) {
-            const cfloat vi = m.v[i];
-            for (int j = i + 1 + lane; j < n; j += 32) {
-                const cfloat u = cphasor(C[i * ldm + j]);
-                const cfloat w = cphasor(cmulc(vi, m.v[j]));
-                const cfloat t = cmulc(u, w);
-                if (!cisnan(t)) {
-                    sre += t.re;
-                    sim += t.im;
-                    ++cnt;
-                }
-            }
-        }
-        sre = warp_sum(sre);
-        sim = warp_sum(sim);
-        cnt = warp_sum_int(cnt);
-        if (lane == 0) {
-            const float fc = (float)cnt;
-            float tc = hypotf(fdiv(sre, fc), fdiv(sim, fc));
-            a.tcoh[p] = isfinite(tc) ? tc : 0.f;
-        }
-    }
-    // CRLB (crlb.py:132-189): X = 2L (Gamma o Gamma^-1 - I), drop `ref`, + 1e-6 I,
-    // sigma = sqrt(diag(FIM^-1)) with 0 inserted at `ref`
-    if (a.compute_crlb) {
-        const int ref = a.crlb_ref, mm = n - 1;
-        float* F = reinterpret_cast<float*>(LU);
-        __syncwarp();
-        for (int e = lane; e < mm * mm; e += 32) {
-            const int ii = e / mm, jj = e - ii * mm;
-            if (jj > ii) continue;
-            const int i = ii + (ii >= ref), j = jj + (jj >= ref);
-            const float x = fmul(a.crlb_factor, fsub(fmul(gamma_reg(a, C, ldm, i, j), G[i * ldg + j]), i == j ? 1.f : 0.f));
-            F[ii * ldg + jj] = ii == jj ? fadd(x, 1e-6f) : x;
-        }
-        __syncwarp();
-        const bool ok = mm > 0 && warp_cholesky(F, ldg, mm, lane);
-        __syncwarp();
-        if (ok) warp_tri_inverse(F, m.Gi, ldg, mm, lane, m.d);
-        __syncwarp();
-        for (int t = lane; t < n; t += 32) {
-            float sg;
-            if (t == ref) sg = 0.f;
-            else sg = ok ? fsqrt(m.d[t - (t > ref)]) : nanf("");
-            a.crlb[p * n + t] = sg;
-        }
-    } else {
-        for (int t = lane; t < n; t += 32) a.crlb[p * n + t] = 0.f;
-    }
-    __syncwarp();
 }
 
 template <int NB, int MODE>
@@ -653,30 +264,34 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
     extern __shared__ __align__(16) unsigned char pix_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     unsigned char* base = pix_smem + warp * a.warp_bytes;
-    Mats m;
+    SolveMats m;
     m.C = reinterpret_cast<cfloat*>(base + a.off_C);
-    m.G = reinterpret_cast<float*>(base + a.off_G);
-    m.Gi = reinterpret_cast<float*>(base + a.off_Gi);
-    m.LU = reinterpret_cast<cfloat*>(base + a.off_LU);
+    m.W1 = reinterpret_cast<float*>(base + a.off_W1);
+    m.R = reinterpret_cast<cfloat*>(base + a.off_S);
+    m.W2 = reinterpret_cast<float*>(base + a.off_W2);
     m.v = reinterpret_cast<cfloat*>(base + a.off_v);
     m.d = reinterpret_cast<float*>(base + a.off_d);
-    m.perm = reinterpret_cast<int*>(base + a.off_perm);
+    m.piv = reinterpret_cast<int*>(base + a.off_piv);
+    const int n = a.n;
     for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
         if (MODE == kSolveOnly) {
-            const cfloat* src = a.Cin + p * a.n * a.n;
-            for (int e = lane; e < a.n * a.n; e += 32) m.C[(e / a.n) * a.ldm + (e % a.n)] = src[e];
+            const cfloat* src = a.Cin + p * n * n;
+            __syncwarp();
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j <= i; j += 32) m.C[pk(i, j)] = src[i * n + j];
             __syncwarp();
         } else {
             int count = 0;
-            warp_covariance<NB>(a, p, m, lane, &count);
+            warp_covariance<NB>(a, p, m.C, m.R, m.d, lane, &count);
             if (a.counts && lane == 0) a.counts[p] = count;
         }
         if (MODE == kCovOnly) {
-            cfloat* dst = a.Cout + p * a.n * a.n;
-            for (int e = lane; e < a.n * a.n; e += 32) dst[e] = m.C[(e / a.n) * a.ldm + (e % a.n)];
+            cfloat* dst = a.Cout + p * n * n;
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j < n; j += 32) dst[i * n + j] = cget(m.C, i, j);
             __syncwarp();
         } else {
-            warp_solve<NB>(a, p, m, lane);
+            solve_pixel<NB>(a, p, m, lane);
         }
     }
 }
@@ -775,17 +390,15 @@ __global__ void __launch_bounds__(256) k_post(PostArgs a) {
 static void fill_pix_layout(PixArgs& a, int n, int wx) {
     PixLayout L = make_layout(n, wx);
     a.n = n;
-    a.ldm = L.ldm;
-    a.ldg = L.ldg;
     a.np = L.np;
     a.stg = L.stg;
     a.off_C = L.off_C;
-    a.off_G = L.off_G;
-    a.off_Gi = L.off_Gi;
-    a.off_LU = L.off_LU;
+    a.off_W1 = L.off_W1;
+    a.off_S = L.off_S;
+    a.off_W2 = L.off_W2;
     a.off_v = L.off_v;
     a.off_d = L.off_d;
-    a.off_perm = L.off_perm;
+    a.off_piv = L.off_piv;
     a.warp_bytes = L.bytes;
 }
 
@@ -801,8 +414,8 @@ static PixTimer g_timer;
 template <int MODE>
 static dpl_status launch_pixel(PixArgs& a, cudaStream_t s);
 
-template <int MODE>
-static dpl_status launch_pixel_timed(PixArgs& a, cudaStream_t s) {
+template <class F>
+static dpl_status timed(cudaStream_t s, F&& launch) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     {
         std::lock_guard<std::mutex> g(g_timer.mu);
@@ -813,7 +426,7 @@ static dpl_status launch_pixel_timed(PixArgs& a, cudaStream_t s) {
         }
     }
     if (e0) DPL_CUDA_TRY(cudaEventRecord(e0, s));
-    dpl_status st = launch_pixel<MODE>(a, s);
+    dpl_status st = launch();
     if (e1) DPL_CUDA_TRY(cudaEventRecord(e1, s));
     return st;
 }
@@ -821,7 +434,8 @@ static dpl_status launch_pixel_timed(PixArgs& a, cudaStream_t s) {
 template <int MODE>
 static dpl_status launch_pixel(PixArgs& a, cudaStream_t s) {
     if (a.npix == 0) return DPL_OK;
-    int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)(110 * 1024) / a.warp_bytes));
+    // as many warps per CTA as fit ~100 KB (two CTAs per SM), at most 8
+    int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)(100 * 1024) / a.warp_bytes));
     size_t smem = (size_t)warps * a.warp_bytes;
     if (smem > 220 * 1024) return fail(DPL_ERR_UNSUPPORTED, "per-pixel shared memory exceeds the SM limit");
     int dev = 0, sms = 0;
@@ -953,7 +567,7 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
         a.tcoh = out->temp_coh;
         a.closure = n > 2 ? out->closure_phases : nullptr;
         a.counts = in->neighbors ? out->shp_counts : nullptr;
-        st = launch_pixel_timed<kFused>(a, s);
+        st = timed(s, [&] { return launch_pixel<kFused>(a, s); });
         if (st != DPL_OK) return st;
 
         PostArgs q{};
@@ -1051,11 +665,17 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
     return launch_pixel<kCovOnly>(a, s);
 }
 
+extern "C" size_t dpl_process_coherence_workspace_size(int64_t npix) {
+    (void)npix;
+    return 256;
+}
+
 extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use_evd, double beta,
                                             double zero_correlation_threshold, int reference_idx, double num_looks,
                                             int first_real_slc_idx, int compute_crlb, float* eig_vecs,
                                             float* eig_vals, uint8_t* estimator, float* crlb_std_dev,
-                                            float* temp_coh, float* closure_phases, dpl_stream_t stream) {
+                                            float* temp_coh, float* closure_phases, void* workspace,
+                                            size_t workspace_bytes, dpl_stream_t stream) {
     if (npix < 0 || nslc <= 0) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence: bad shape");
     if (nslc > kMaxNslc) return fail(DPL_ERR_UNSUPPORTED, "at most 64 SLCs per call are supported");
     if (npix == 0) return DPL_OK;
@@ -1074,6 +694,8 @@ extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int ns
     a.crlb = crlb_std_dev;
     a.tcoh = temp_coh;
     a.closure = nslc > 2 ? closure_phases : nullptr;
+    (void)workspace;
+    (void)workspace_bytes;
     return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream);
 }
 

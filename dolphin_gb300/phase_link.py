@@ -205,11 +205,12 @@ def process_coherence_matrices(C_arrays, use_evd: bool = False, beta: float = 0.
     clos = D.empty((npix, max(n - 2, 0)), np.float32)
     lib = _lib.load()
     ref = reference_idx + n if reference_idx < 0 else reference_idx
+    ws = D.workspace(lib.dpl_process_coherence_workspace_size(npix))
     st = lib.dpl_process_coherence(D.ptr(Cd), npix, n, int(bool(use_evd)), float(beta),
                                    float(zero_correlation_threshold), int(ref), float(num_looks),
                                    int(first_real_slc_idx), int(bool(compute_crlb)), D.ptr(vec), D.ptr(val),
                                    D.ptr(est), D.ptr(crlb), D.ptr(tc), D.ptr(clos) if n > 2 else None,
-                                   D.stream_handle())
+                                   D.ptr(ws), ws.numel(), D.stream_handle())
     _lib.check(st, "dpl_process_coherence")
     outs = [vec.reshape(*batch, n), val.reshape(batch), est.reshape(batch), crlb.reshape(*batch, n)]
     if return_metrics:

@@ -157,13 +157,15 @@ dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t rows, int64_t 
  * eig_vals     : (npix) float32;  estimator : (npix) uint8
  * crlb_std_dev : (npix, nslc) float32 (zeros if !compute_crlb)
  * temp_coh     : (npix) float32;  closure_phases : (npix, nslc - 2) float32 or NULL
- * num_looks    : sqrt(hy * hx) in the reference */
+ * num_looks    : sqrt(hy * hx) in the reference
+ * workspace    : dpl_process_coherence_workspace_size(npix) bytes */
+size_t dpl_process_coherence_workspace_size(int64_t npix);
 dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use_evd, double beta,
                                  double zero_correlation_threshold, int reference_idx,
                                  double num_looks, int first_real_slc_idx, int compute_crlb,
                                  float* eig_vecs, float* eig_vals, uint8_t* estimator,
                                  float* crlb_std_dev, float* temp_coh, float* closure_phases,
-                                 dpl_stream_t stream);
+                                 void* workspace, size_t workspace_bytes, dpl_stream_t stream);
 
 /* Timing of the per-pixel phase-linking kernel (no reference counterpart: a
  * measurement hook).  While enabled, dpl_phase_link records a CUDA event pair on
