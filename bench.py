@@ -232,8 +232,8 @@ def run_ours(args, rank, world, pool, cores):
     # ---- device-resident timed region ----
     sampler = ClockSampler(local)
     sampler.start()
-    tot = _lib.C.c_double()
-    cnt = _lib.C.c_int64()
+    tot = (_lib.C.c_double * 2)()
+    cnt = (_lib.C.c_int64 * 2)()
     lib.dpl_kernel_timing(1, tot, cnt)
     barrier()
     torch.cuda.synchronize()
@@ -248,8 +248,9 @@ def run_ours(args, rank, world, pool, cores):
     lib.dpl_kernel_timing(0, tot, cnt)
     clocks = sampler.stop()
     ms = e0.elapsed_time(e1) / args.steps
-    kern_ms = tot.value / max(cnt.value, 1)
-    kern_launches_per_step = cnt.value / args.steps
+    cov_ms = tot[0] / max(cnt[0], 1)   # per launch (one launch per block)
+    sol_ms = tot[1] / max(cnt[1], 1)
+    launches_cov = cnt[0] / args.steps
 
     # ---- end-to-end: pinned host stack in, host results out, through the public API ----
     host_stack = torch.empty(stack.shape, dtype=stack.dtype, pin_memory=True)
@@ -284,19 +285,24 @@ def run_ours(args, rank, world, pool, cores):
     d2h = host_cpx.numel() * host_cpx.element_size() + host_tc.numel() * host_tc.element_size()
 
     # max over ranks
-    vals = torch.tensor([ms, e2e_ms, kern_ms], dtype=torch.float64, device=dev)
+    vals = torch.tensor([ms, e2e_ms, cov_ms, sol_ms], dtype=torch.float64, device=dev)
     if dist is not None:
         dist.all_reduce(vals, op=dist.ReduceOp.MAX)
-    ms, e2e_ms, kern_ms = vals.tolist()
+    ms, e2e_ms, cov_ms, sol_ms = vals.tolist()
     if rank != 0:
         return
     px = frame * frame * world
     value = px / (ms / 1000.0)
-    # roofline of the dominant kernel (per-pixel covariance + solver): algorithmic flops
+    # roofline of the covariance contraction (tensor cores): algorithmic flops
+    # F_cov = 4 W N (N + 1) per output pixel (Hermitian half, complex MAC = 8 flops)
     W = (2 * HALF[0] + 1) * (2 * HALF[1] + 1)
     f_cov = 4.0 * W * NSLC * (NSLC + 1)
     px_per_launch = sum((ir[1] - ir[0]) * (ic[1] - ic[0]) for (ir, ic, *_r) in plan) / len(plan)
-    achieved = f_cov * px_per_launch / (kern_ms / 1000.0) / 1e12
+    achieved = f_cov * px_per_launch / (cov_ms / 1000.0) / 1e12
+    # solver flops per pixel (EMI): Cholesky + inverse of |Gamma| (~N^3), complex
+    # Cholesky of A - 0.99 I (4N^3/3), ~7 inverse iterations (8N^2 each), CRLB (~2N^3/3)
+    f_sol = NSLC**3 * (1.0 + 4.0 / 3.0 + 2.0 / 3.0) + 7 * 8.0 * NSLC**2
+    fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -308,7 +314,7 @@ def run_ours(args, rank, world, pool, cores):
         cv, cd = cpu_sample(pool, cores)
         cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": cd + " (numpy restatement of the reference algorithm)"}
-    launches_per_step = len(plan) * 6  # k_ps_block, k_glrt_scale, k_glrt, k_prep, k_pixel, k_post
+    launches_per_step = len(plan) * 7  # k_ps_block, k_glrt_scale, k_glrt, k_prep, k_cov_tc, k_pixel, k_post
     line = {
         "metric": METRIC,
         "value": value,
@@ -324,15 +330,20 @@ def run_ours(args, rank, world, pool, cores):
         "data": "synthetic",
         "config": {"workload": f"N={NSLC} {frame}x{frame} stack per GPU, {BLOCK}x{BLOCK} blocks with halo, "
                                f"half-window {HALF}, GLRT {ALPHA}, EMI, PS {PS_THR} + fill, CRLB",
-                   "l2": "inputs larger than L2 (4 GB stack per GPU)", "form": "plain (FP32 SIMT covariance)"},
+                   "l2": "inputs larger than L2 (4 GB stack per GPU)",
+                   "form": "chosen: tensor-core covariance (bf16 hi/lo, fp32 accumulate) + FP32 solver"},
         "e2e": {"value": px / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_per_step * args.steps),
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "k_pixel", "kernel_ms": kern_ms,
-                     "launches_per_step": kern_launches_per_step,
-                     "note": "algorithmic covariance flops 4*W*N*(N+1) per pixel over the measured launch time; "
-                             "peak = measured bf16 dense (MEASURED_PEAKS.json)"},
+                     "kernel": "k_cov_tc", "kernel_ms": cov_ms, "launches_per_step": launches_cov,
+                     "note": "algorithmic covariance flops 4*W*N*(N+1) per pixel over the measured launch time "
+                             "(CUDA events on the launch stream); peak = measured bf16 dense (of measured)"},
+        "solver": {"kernel": "k_pixel (solve)", "kernel_ms": sol_ms,
+                   "achieved_tflops": f_sol * px_per_launch / (sol_ms / 1000.0) / 1e12 if sol_ms > 0 else None,
+                   "fp32_nominal_tflops": fp32_nominal,
+                   "note": "FP32 CUDA-core bound; algorithmic flops ~(3N^3 + 56N^2) per pixel; nominal peak, "
+                           "no measured FP32 figure"},
         "clocks": clocks,
     }
     if cpu:

@@ -36,7 +36,7 @@ class PlParams(C.Structure):
         ("hy", _i), ("hx", _i), ("sy", _i), ("sx", _i),
         ("use_evd", _i), ("beta", _d), ("zero_correlation_threshold", _d),
         ("reference_idx", _i), ("mask_input_ps", _i), ("use_max_ps", _i), ("use_slc_amp", _i),
-        ("baseline_lag", _i), ("first_real_slc_idx", _i), ("compute_crlb", _i),
+        ("baseline_lag", _i), ("first_real_slc_idx", _i), ("compute_crlb", _i), ("cov_form", _i),
     ]
 
 
@@ -63,7 +63,7 @@ SIGNATURES = {
     "dpl_phase_link_workspace_size": (_sz, [C.POINTER(PlParams)]),
     "dpl_phase_link": (_i, [C.POINTER(PlParams), C.POINTER(PlInputs), C.POINTER(PlOutputs), _p, _sz, _p]),
     "dpl_covariance_workspace_size": (_sz, [_i64, _i64, _i64]),
-    "dpl_covariance": (_i, [_p, _i64, _i64, _i64, _i, _i, _i, _i, _p, _p, _p, _sz, _p]),
+    "dpl_covariance": (_i, [_p, _i64, _i64, _i64, _i, _i, _i, _i, _p, _i, _p, _p, _sz, _p]),
     "dpl_process_coherence_workspace_size": (_sz, [_i64]),
     "dpl_process_coherence": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _sz, _p]),
     "dpl_kernel_timing": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

@@ -153,6 +153,7 @@ struct PixArgs {
     const uint32_t* nb_bits; // (out_rows, out_cols, wy, wpr) or null
     int wpr;
     const cfloat* Cin;       // solve-only input: (npix, n, n)
+    const float* Cplanar;    // solve-only input, planar per pixel: diag Re | off-diag Re | off-diag Im
     int use_evd, beta_on;
     float one_minus_beta, beta, zct;
     int ref_idx, compute_crlb, crlb_ref, baseline_lag;
@@ -275,10 +276,20 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
     const int n = a.n;
     for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
         if (MODE == kSolveOnly) {
-            const cfloat* src = a.Cin + p * n * n;
             __syncwarp();
-            for (int i = 0; i < n; ++i)
-                for (int j = lane; j <= i; j += 32) m.C[pk(i, j)] = src[i * n + j];
+            if (a.Cplanar) {
+                const float* src = a.Cplanar + p * n * n;
+                const int O = n * (n - 1) / 2;
+                for (int i = 0; i < n; ++i)
+                    for (int j = lane; j <= i; j += 32) {
+                        const int o = i * (i - 1) / 2 + j;  // pair (i, j), i > j
+                        m.C[pk(i, j)] = i == j ? cmake(src[i], 0.f) : cmake(src[n + o], src[n + O + o]);
+                    }
+            } else {
+                const cfloat* src = a.Cin + p * n * n;
+                for (int i = 0; i < n; ++i)
+                    for (int j = lane; j <= i; j += 32) m.C[pk(i, j)] = src[i * n + j];
+            }
             __syncwarp();
         } else {
             int count = 0;
@@ -294,6 +305,28 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
             solve_pixel<NB>(a, p, m, lane);
         }
     }
+}
+
+}  // namespace dpl
+
+#include "cov_tc.cuh"
+
+namespace dpl {
+
+// planar coherence (tensor-core layout) -> full (npix, n, n) complex
+__global__ void k_unpack_planar(const float* __restrict__ Cg, int n, int64_t npix, cfloat* __restrict__ out) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nn = (int64_t)n * n;
+    if (e >= npix * nn) return;
+    const int64_t p = e / nn;
+    const int r = (int)(e - p * nn), i = r / n, j = r - i * n;
+    const float* src = Cg + p * nn;
+    const int O = n * (n - 1) / 2;
+    cfloat v;
+    if (i == j) v = cmake(src[i], 0.f);
+    else if (i > j) v = cmake(src[n + i * (i - 1) / 2 + j], src[n + O + i * (i - 1) / 2 + j]);
+    else v = cmake(src[n + j * (j - 1) / 2 + i], -src[n + O + j * (j - 1) / 2 + i]);
+    out[e] = v;
 }
 
 // ---------------------------------------------------------------------------------
@@ -407,7 +440,7 @@ static void fill_pix_layout(PixArgs& a, int n, int wx) {
 struct PixTimer {
     std::mutex mu;
     bool on = false;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[2];  // [0] covariance, [1] solver
 };
 static PixTimer g_timer;
 
@@ -415,14 +448,14 @@ template <int MODE>
 static dpl_status launch_pixel(PixArgs& a, cudaStream_t s);
 
 template <class F>
-static dpl_status timed(cudaStream_t s, F&& launch) {
+static dpl_status timed(cudaStream_t s, int slot, F&& launch) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     {
         std::lock_guard<std::mutex> g(g_timer.mu);
         if (g_timer.on) {
             DPL_CUDA_TRY(cudaEventCreate(&e0));
             DPL_CUDA_TRY(cudaEventCreate(&e1));
-            g_timer.ev.emplace_back(e0, e1);
+            g_timer.ev[slot].emplace_back(e0, e1);
         }
     }
     if (e0) DPL_CUDA_TRY(cudaEventRecord(e0, s));
@@ -454,6 +487,74 @@ static dpl_status launch_pixel(PixArgs& a, cudaStream_t s) {
     return go(k_pixel<2, MODE>);
 }
 
+// Tensor-core covariance: fills `Cg` (npix x n*n planar floats).
+static size_t tc_cov_bytes(int n, int64_t out_rows, int64_t out_cols) {
+    return (size_t)out_rows * out_cols * n * n * sizeof(float);
+}
+
+static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int sy, int sx, const cfloat* zt,
+                                const uint32_t* bits, int wpr, const uint8_t* nb_u8, float* Cg, int32_t* counts,
+                                int* status, cudaStream_t s) {
+    TcArgs a{};
+    a.n = n;
+    a.rows = rows;
+    a.cols = cols;
+    a.hy = hy;
+    a.hx = hx;
+    a.sy = sy;
+    a.sx = sx;
+    a.out_rows = rows / sy;
+    a.out_cols = cols / sx;
+    if (a.out_rows == 0 || a.out_cols == 0) return DPL_OK;
+    const int wy = 2 * hy + 1, wx = 2 * hx + 1;
+    a.tile_r = 8;
+    a.tile_c = 16;
+    a.tiles_r = ceil_div(a.out_rows, a.tile_r);
+    a.tiles_c = ceil_div(a.out_cols, a.tile_c);
+    a.region_r = (a.tile_r - 1) * sy + wy;
+    a.region_c = (a.tile_c - 1) * sx + wx;
+    a.kpad = ceil_div((int64_t)a.region_r * a.region_c, kTcKC) * kTcKC;
+    const int nn = n * n;
+    a.npass = ceil_div(nn, kTcMaxPW);
+    a.pw = ceil_div(ceil_div(nn, a.npass), 16) * 16;
+    if (a.pw > kTcMaxPW || a.pw < n) return fail(DPL_ERR_UNSUPPORTED, "tensor-core covariance: unsupported N");
+    a.zt = zt;
+    a.bits = bits;
+    a.wpr = wpr;
+    a.nb_u8 = nb_u8;
+    a.Cg = Cg;
+    a.counts = counts;
+    a.status = status;
+    size_t o = 0;
+    auto take = [&](size_t bytes, size_t al) {
+        o = align_up(o, al);
+        size_t at = o;
+        o += bytes;
+        return (int)at;
+    };
+    a.stage_a_bytes = kTcM * kTcKC * 2;
+    a.stage_b_bytes = 2 * a.pw * kTcKC * 2;
+    const size_t stage = (size_t)a.stage_a_bytes + a.stage_b_bytes;
+    a.off_stage0 = take(std::max(stage, (size_t)kTcM * 33 * 4), 1024);
+    a.off_stage1 = take(stage, 1024);
+    a.off_z = take((size_t)kTcKC * n * sizeof(cfloat), 16);
+    a.off_amp = take((size_t)kTcM * (n + 1) * sizeof(float), 16);
+    a.off_col = take((size_t)a.npass * a.pw * sizeof(uint32_t), 16);
+    a.off_mask = take((size_t)kTcM * wy * 2 * sizeof(uint32_t), 16);
+    a.off_win = take((size_t)kTcM * 2 * sizeof(int), 16);
+    a.off_bar = take(128, 64);
+    a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
+    if (a.smem_bytes > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "tensor-core covariance: window too large");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes));
+    const int ntiles = a.tiles_r * a.tiles_c;
+    const int grid = std::max(1, std::min(ntiles, sms));
+    k_cov_tc<<<grid, kTcThreads, a.smem_bytes, s>>>(a);
+    return check_launch("k_cov_tc");
+}
+
 static int norm_ref(int ref, int n) { return ref < 0 ? n + ref : ref; }
 
 static void set_solver_params(PixArgs& a, int use_evd, double beta, double zct, int ref_idx, double num_looks,
@@ -472,6 +573,7 @@ static void set_solver_params(PixArgs& a, int use_evd, double beta, double zct, 
 struct PlWorkspace {
     int* status;
     unsigned int* valid_bits;
+    float* Cg;
     uint8_t* flags;
     float* avgmag;
     cfloat* zt;
@@ -479,12 +581,14 @@ struct PlWorkspace {
     float* CR;
 };
 
-static size_t pl_workspace_layout(int64_t n, int64_t rows, int64_t cols, int sy, int sx, char* base, PlWorkspace* w) {
+static size_t pl_workspace_layout(int64_t n, int64_t rows, int64_t cols, int sy, int sx, int cov_form, char* base,
+                                  PlWorkspace* w) {
     Workspace ws{base, ~size_t(0)};
     const int64_t npix = rows * cols, P = (rows / sy) * (cols / sx);
     PlWorkspace t{};
     t.status = ws.take<int>(16);
     t.valid_bits = ws.take<unsigned int>(16);
+    t.Cg = cov_form == 0 ? ws.take<float>(P * n * n) : nullptr;
     t.flags = ws.take<uint8_t>(npix);
     t.avgmag = ws.take<float>(npix);
     t.zt = ws.take<cfloat>(npix * n);
@@ -511,7 +615,8 @@ using namespace dpl;
 
 extern "C" size_t dpl_phase_link_workspace_size(const dpl_pl_params* p) {
     if (!p) return 0;
-    return pl_workspace_layout(p->nslc, p->rows, p->cols, std::max(1, p->sy), std::max(1, p->sx), nullptr, nullptr);
+    return pl_workspace_layout(p->nslc, p->rows, p->cols, std::max(1, p->sy), std::max(1, p->sx), p->cov_form, nullptr,
+                               nullptr);
 }
 
 extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
@@ -525,10 +630,11 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
     const int n = (int)P.nslc;
     const int ref = norm_ref(P.reference_idx, n);
     if (ref < 0 || ref >= n) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
+    if (P.cov_form != 0 && P.cov_form != 1) return fail(DPL_ERR_INVALID_ARGUMENT, "cov_form must be 0 or 1");
     if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
     PlWorkspace w;
-    pl_workspace_layout(P.nslc, P.rows, P.cols, P.sy, P.sx, (char*)workspace, &w);
+    pl_workspace_layout(P.nslc, P.rows, P.cols, P.sy, P.sx, P.cov_form, (char*)workspace, &w);
     const int64_t npix = P.rows * P.cols;
     const int out_rows = (int)(P.rows / P.sy), out_cols = (int)(P.cols / P.sx);
     const int64_t Pout = (int64_t)out_rows * out_cols;
@@ -567,7 +673,19 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
         a.tcoh = out->temp_coh;
         a.closure = n > 2 ? out->closure_phases : nullptr;
         a.counts = in->neighbors ? out->shp_counts : nullptr;
-        st = timed(s, [&] { return launch_pixel<kFused>(a, s); });
+        if (P.cov_form == 0) {
+            // chosen form: tensor-core covariance, then the solver on the planar matrices
+            st = timed(s, 0, [&] {
+                return launch_cov_tc(n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, w.zt, nullptr, 0,
+                                     in->neighbors, w.Cg, a.counts, w.status, s);
+            });
+            if (st != DPL_OK) return st;
+            a.Cplanar = w.Cg;
+            st = timed(s, 1, [&] { return launch_pixel<kSolveOnly>(a, s); });
+        } else {
+            // plain form: SIMT covariance fused with the solver
+            st = timed(s, 0, [&] { return launch_pixel<kFused>(a, s); });
+        }
         if (st != DPL_OK) return st;
 
         PostArgs q{};
@@ -622,12 +740,13 @@ extern "C" size_t dpl_covariance_workspace_size(int64_t nslc, int64_t rows, int6
     ws.take<unsigned int>(16);
     ws.take<uint8_t>(rows * cols);
     ws.take<cfloat>(rows * cols * nslc);
+    ws.take<float>(rows * cols * nslc * nslc);  // planar matrices of the tensor-core form (strides >= 1)
     return align_up(ws.used, 256);
 }
 
 extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t rows, int64_t cols, int hy, int hx,
-                                     int sy, int sx, const uint8_t* neighbors, float* C, void* workspace,
-                                     size_t workspace_bytes, dpl_stream_t stream) {
+                                     int sy, int sx, const uint8_t* neighbors, int cov_form, float* C,
+                                     void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
     dpl_status st = validate_common(nslc, rows, cols, hy, hx, sy, sx);
     if (st != DPL_OK) return st;
     if (!slc || !C || !workspace) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: null pointer");
@@ -640,7 +759,7 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
     unsigned int* vb = ws.take<unsigned int>(16);
     uint8_t* flags = ws.take<uint8_t>(rows * cols);
     cfloat* zt = ws.take<cfloat>(rows * cols * nslc);
-    (void)status;
+    float* Cg = ws.take<float>(rows * cols * nslc * nslc);
     const int64_t npix = rows * cols;
     size_t smem = (size_t)kPrepPix * (n + 1) * sizeof(cfloat);
     DPL_CUDA_TRY(cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -662,7 +781,13 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
     a.zt = zt;
     a.nb_u8 = neighbors;
     a.Cout = reinterpret_cast<cfloat*>(C);
-    return launch_pixel<kCovOnly>(a, s);
+    if (cov_form == 1) return launch_pixel<kCovOnly>(a, s);
+    DPL_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
+    st = launch_cov_tc(n, (int)rows, (int)cols, hy, hx, sy, sx, zt, nullptr, 0, neighbors, Cg, nullptr, status, s);
+    if (st != DPL_OK) return st;
+    const int64_t tot = a.npix * n * n;
+    k_unpack_planar<<<ceil_div(tot, 256), 256, 0, s>>>(Cg, n, a.npix, reinterpret_cast<cfloat*>(C));
+    return check_launch("k_unpack_planar");
 }
 
 extern "C" size_t dpl_process_coherence_workspace_size(int64_t npix) {
@@ -701,20 +826,23 @@ extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int ns
 
 extern "C" dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches) {
     std::lock_guard<std::mutex> g(g_timer.mu);
-    double tot = 0.0;
-    int64_t cnt = 0;
-    for (auto& pr : g_timer.ev) {
-        float ms = 0.f;
-        if (cudaEventSynchronize(pr.second) == cudaSuccess && cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
-            tot += ms;
-            ++cnt;
+    for (int slot = 0; slot < 2; ++slot) {
+        double tot = 0.0;
+        int64_t cnt = 0;
+        for (auto& pr : g_timer.ev[slot]) {
+            float ms = 0.f;
+            if (cudaEventSynchronize(pr.second) == cudaSuccess &&
+                cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
+                tot += ms;
+                ++cnt;
+            }
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
         }
-        cudaEventDestroy(pr.first);
-        cudaEventDestroy(pr.second);
+        g_timer.ev[slot].clear();
+        if (total_ms) total_ms[slot] = tot;
+        if (launches) launches[slot] = cnt;
     }
-    g_timer.ev.clear();
     g_timer.on = enable != 0;
-    if (total_ms) *total_ms = tot;
-    if (launches) *launches = cnt;
     return DPL_OK;
 }

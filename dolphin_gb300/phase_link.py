@@ -84,11 +84,17 @@ def run_phase_linking(
     baseline_lag: Optional[int] = None,
     first_real_slc_idx: int = 0,
     compute_crlb: bool = True,
+    *,
+    covariance_form: str = "tensor",
 ) -> PhaseLinkOutput:
     """Estimate the linked phase for a stack of SLCs (phase_link/_core.py:67-249).
 
     Host (numpy) inputs give numpy outputs; if ``slc_stack`` is a CUDA tensor, all
     outputs stay on the device as tensors (``estimator`` uint8, masks uint8).
+
+    ``covariance_form`` (keyword-only, not in the reference): ``"tensor"`` computes
+    the coherence matrices on the tensor cores (bf16 hi/lo split, fp32
+    accumulation); ``"simt"`` uses fp32 CUDA-core arithmetic throughout.
     """
     on_device = D.is_device_tensor(slc_stack)
     shape = tuple(slc_stack.shape)
@@ -128,6 +134,7 @@ def run_phase_linking(
         use_max_ps=int(bool(use_max_ps)), use_slc_amp=int(bool(use_slc_amp)),
         baseline_lag=int(baseline_lag) if baseline_lag else 0,
         first_real_slc_idx=int(first_real_slc_idx), compute_crlb=int(bool(compute_crlb)),
+        cov_form=_form_code(covariance_form),
     )
     cpx = D.empty((nslc, out_rows, out_cols), np.complex64)
     tcoh = D.empty((out_rows, out_cols), np.float32)
@@ -160,8 +167,15 @@ def run_phase_linking(
     )
 
 
+def _form_code(form: str) -> int:
+    codes = {"tensor": 0, "simt": 1}
+    if form not in codes:
+        raise ValueError(f"covariance_form must be one of {sorted(codes)}, got {form!r}")
+    return codes[form]
+
+
 def estimate_stack_covariance(slc_stack, half_window: HalfWindow, strides: Strides = DEFAULT_STRIDES,
-                              neighbor_arrays=None):
+                              neighbor_arrays=None, *, covariance_form: str = "tensor"):
     """SHP-masked coherence matrices (covariance.py:24-107): (rows', cols', N, N) complex64."""
     if not _is_complex(slc_stack):
         raise ValueError("The SLC stack must be complex.")
@@ -175,8 +189,8 @@ def estimate_stack_covariance(slc_stack, half_window: HalfWindow, strides: Strid
     C = D.empty((out_rows, out_cols, nslc, nslc), np.complex64)
     lib = _lib.load()
     ws = D.workspace(lib.dpl_covariance_workspace_size(nslc, rows, cols))
-    st = lib.dpl_covariance(D.ptr(slc), nslc, rows, cols, hy, hx, sy, sx, D.ptr(nb), D.ptr(C), D.ptr(ws),
-                            ws.numel(), D.stream_handle())
+    st = lib.dpl_covariance(D.ptr(slc), nslc, rows, cols, hy, hx, sy, sx, D.ptr(nb), _form_code(covariance_form),
+                            D.ptr(C), D.ptr(ws), ws.numel(), D.stream_handle())
     _lib.check(st, "dpl_covariance")
     return C if on_device else D.to_host(C)
 

@@ -108,6 +108,7 @@ typedef struct dpl_pl_params {
     int baseline_lag;              /* <= 0: off */
     int first_real_slc_idx;
     int compute_crlb;
+    int cov_form;                  /* 0: tensor-core covariance (default); 1: SIMT covariance (plain form) */
 } dpl_pl_params;
 
 typedef struct dpl_pl_inputs {
@@ -146,7 +147,7 @@ dpl_status dpl_phase_link(const dpl_pl_params* params, const dpl_pl_inputs* inpu
  * C : (out_rows, out_cols, nslc, nslc) complex64 out.  NaN samples are masked. */
 size_t dpl_covariance_workspace_size(int64_t nslc, int64_t rows, int64_t cols);
 dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t rows, int64_t cols, int hy,
-                          int hx, int sy, int sx, const uint8_t* neighbors, float* C,
+                          int hx, int sy, int sx, const uint8_t* neighbors, int cov_form, float* C,
                           void* workspace, size_t workspace_bytes, dpl_stream_t stream);
 
 /* Replaces: _core.process_coherence_matrices(C_arrays, ...) -- phase_link/_core.py:379-534,
@@ -167,11 +168,12 @@ dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use
                                  float* crlb_std_dev, float* temp_coh, float* closure_phases,
                                  void* workspace, size_t workspace_bytes, dpl_stream_t stream);
 
-/* Timing of the per-pixel phase-linking kernel (no reference counterpart: a
- * measurement hook).  While enabled, dpl_phase_link records a CUDA event pair on
- * its stream around each launch of that kernel.  Each call returns (and clears)
- * the summed elapsed milliseconds and launch count of the pairs recorded since the
- * previous call, waiting for them to complete, then sets the enable state. */
+/* Kernel timing (no reference counterpart: a measurement hook).  While enabled,
+ * dpl_phase_link records CUDA event pairs on its stream around the covariance
+ * kernel (slot 0) and the solver kernel (slot 1; the plain form fuses both into
+ * slot 0).  Each call returns (and clears) per slot the summed elapsed milliseconds
+ * and launch counts recorded since the previous call -- total_ms[2], launches[2] --
+ * waiting for them to complete, then sets the enable state. */
 dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches);
 
 #ifdef __cplusplus

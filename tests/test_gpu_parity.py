@@ -146,21 +146,46 @@ def test_ks_requires_amp_stack():
 # ---------------------------------------------------------------------------------
 # covariance
 # ---------------------------------------------------------------------------------
-def test_covariance_golden(golden):
+# fp32 SIMT sums vs bf16 hi/lo products with fp32 accumulation
+COV_ATOL = {"simt": 5e-6, "tensor": 3e-5}
+
+
+@pytest.mark.parametrize("form", ["tensor", "simt"])
+def test_covariance_golden(golden, form):
     g = golden("covariance")
     z = g["slc"]
-    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (1, 1)), g["C_rect"], atol=2e-6)
-    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (1, 1), g["nb"]), g["C_nb"], atol=2e-6)
-    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (2, 3)), g["C_strided"], atol=2e-6)
+    tol = COV_ATOL[form]
+    kw = dict(covariance_form=form)
+    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (1, 1), **kw), g["C_rect"], atol=tol)
+    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (1, 1), g["nb"], **kw), g["C_nb"], atol=tol)
+    np.testing.assert_allclose(dp.estimate_stack_covariance(z, (3, 4), (2, 3), **kw), g["C_strided"], atol=tol)
 
 
-@pytest.mark.parametrize("n", [3, 20, 33, 64])
-def test_covariance_vs_float64(n):
+@pytest.mark.parametrize("form", ["tensor", "simt"])
+@pytest.mark.parametrize("n", [3, 20, 30, 33, 64])
+def test_covariance_vs_float64(n, form):
     z = make_stack(StackConfig(nslc=n, rows=19, cols=27, seed=n, ps_frac=0.0))
     z[1, 4, 5] = np.nan
-    got = dp.estimate_stack_covariance(z, (2, 3), (1, 2))
+    got = dp.estimate_stack_covariance(z, (2, 3), (1, 2), covariance_form=form)
     ref = O.estimate_stack_covariance(z.astype(np.complex128), (2, 3), (1, 2), dtype=np.float64)
-    np.testing.assert_allclose(got, ref, atol=5e-6)
+    np.testing.assert_allclose(got, ref, atol=COV_ATOL[form])
+
+
+@pytest.mark.parametrize("form", ["tensor", "simt"])
+def test_covariance_with_shp_masks(form):
+    """Masks with holes and a PS-like bright pixel, large window (5, 11), tile edges."""
+    z = make_stack(StackConfig(nslc=30, rows=37, cols=70, seed=9, ps_frac=0.03))
+    amp = np.abs(z)
+    mean, disp, ps = O.calc_ps_block(amp, 0.25, 30)
+    nb = O.estimate_neighbors_glrt(mean, (disp * mean) ** 2, (5, 11), (1, 1), 30, 0.001)
+    got = dp.estimate_stack_covariance(z, (5, 11), (1, 1), nb, covariance_form=form)
+    ref = O.estimate_stack_covariance(z.astype(np.complex128), (5, 11), (1, 1), nb, dtype=np.float64)
+    np.testing.assert_allclose(got, ref, atol=COV_ATOL[form])
+
+
+def test_covariance_form_rejects_unknown():
+    with pytest.raises(ValueError):
+        dp.estimate_stack_covariance(np.ones((3, 5, 5), np.complex64), (1, 1), covariance_form="nope")
 
 
 def test_covariance_rejects_real():
@@ -247,7 +272,14 @@ def test_singular_gamma_falls_back_to_evd():
 # ---------------------------------------------------------------------------------
 # run_phase_linking end to end
 # ---------------------------------------------------------------------------------
-def test_run_phase_linking_golden_cases(golden):
+# |Gamma| + 1e-6 I closer to singular than this (float64 smallest eigenvalue) decides
+# EMI vs EVD by rounding: the tensor form perturbs C by ~1e-5, i.e. lambda_min by up
+# to ~N * 1e-5, so its band is wider.
+BORDER = {"simt": 1e-4, "tensor": 1e-3}
+
+
+@pytest.mark.parametrize("form", ["tensor", "simt"])
+def test_run_phase_linking_golden_cases(golden, form):
     g = golden("phase_link")
     specs = ast.literal_eval(str(g["specs"][0]))
     for idx, (zname, hw, strides, kw) in specs.items():
@@ -255,17 +287,22 @@ def test_run_phase_linking_golden_cases(golden):
         for key in ("ps_mask", "nodata_mask", "neighbor_arrays", "avg_mag"):
             if key in kw:
                 kw[key] = np.array(g[kw[key]])
-        out = dp.run_phase_linking(np.array(g[zname]), hw, strides, **kw)
-        compare_pl(out, g, idx)
+        diag = {}
+        okw = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in kw.items()}
+        O.run_phase_linking(np.array(g[zname]), hw, strides, diagnostics=diag, **okw)
+        out = dp.run_phase_linking(np.array(g[zname]), hw, strides, covariance_form=form, **kw)
+        compare_pl(out, g, idx, borderline=diag["gamma_min_eig"] < BORDER[form])
 
 
-def test_config1_crop_golden(golden):
+@pytest.mark.parametrize("form", ["tensor", "simt"])
+def test_config1_crop_golden(golden, form):
     g = golden("config1_crop")
     diag = {}
     O.run_phase_linking(g["slc"], (5, 5), (1, 1), ps_mask=g["ps"].copy(), neighbor_arrays=g["nb"],
                         avg_mag=g["mean"], diagnostics=diag)
-    out = dp.run_phase_linking(g["slc"], (5, 5), ps_mask=g["ps"], neighbor_arrays=g["nb"], avg_mag=g["mean"])
-    compare_pl(out, g, "emi", borderline=diag["gamma_min_eig"] < 1e-4)
+    out = dp.run_phase_linking(g["slc"], (5, 5), ps_mask=g["ps"], neighbor_arrays=g["nb"], avg_mag=g["mean"],
+                               covariance_form=form)
+    compare_pl(out, g, "emi", borderline=diag["gamma_min_eig"] < BORDER[form])
 
 
 @pytest.mark.parametrize("strides", [1, 2, 3, 4, 5])
@@ -283,18 +320,19 @@ def test_strides_window_sizes(strides, half_window, shape):
     assert out.cpx_phase.shape == (4, shape[0] // strides, shape[1] // strides)
 
 
-def test_config1_full_vs_oracle_f32_and_f64():
+@pytest.mark.parametrize("form", ["tensor", "simt"])
+def test_config1_full_vs_oracle_f32_and_f64(form):
     """Config 1 (N=10, 128x128, hw 5x5, GLRT 0.001, EMI, PS 0.25) against both oracles."""
     z = make_stack(StackConfig())
     amp = np.abs(z)
     mean, disp, ps = dp.calc_ps_block(amp, 0.25, 10)
     var = (disp * mean) ** 2
     nb = dp.estimate_neighbors(halfwin_rowcol=(5, 5), alpha=0.001, mean=mean, var=var, nslc=10)
-    out = dp.run_phase_linking(z, (5, 5), ps_mask=ps, neighbor_arrays=nb, avg_mag=mean)
+    out = dp.run_phase_linking(z, (5, 5), ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, covariance_form=form)
     diag = {}
     ref = O.run_phase_linking(z, (5, 5), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, diagnostics=diag)
     ref64 = O.run_phase_linking(z, (5, 5), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, dtype=np.float64)
-    border = diag["gamma_min_eig"] < 1e-4
+    border = diag["gamma_min_eig"] < BORDER[form]
     np.testing.assert_array_equal(out.estimator[~border], ref.estimator[~border])
     good = (ref.temp_coh > 0.3) & ~border & np.all(np.isfinite(ref.cpx_phase), axis=0)
     assert good.mean() > 0.5
@@ -369,3 +407,22 @@ def test_device_tensors_stay_on_device():
     assert out.cpx_phase.is_cuda and out.temp_coh.is_cuda
     host = dp.run_phase_linking(z, (2, 2))
     np.testing.assert_array_equal(out.cpx_phase.cpu().numpy(), host.cpx_phase)
+
+
+def test_config2_crop_tensor_vs_float64():
+    """Config 2 parameters (N=30, half-window (5, 11), GLRT 0.001, EMI, PS 0.25, CRLB) on a
+    64 x 96 crop: chosen (tensor) form against the float64 oracle, 1e-3 rad / 1e-4."""
+    z = make_stack(StackConfig(nslc=30, rows=64 + 10, cols=96 + 22, seed=20261205, ps_frac=0.03))
+    mean, disp, ps = dp.calc_ps_block(np.abs(z), 0.25, 30)
+    nb = dp.estimate_neighbors(halfwin_rowcol=(5, 11), alpha=0.001, mean=mean, var=(disp * mean) ** 2, nslc=30)
+    out = dp.run_phase_linking(z, (5, 11), ps_mask=ps, neighbor_arrays=nb, avg_mag=mean)
+    diag = {}
+    ref64 = O.run_phase_linking(z, (5, 11), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean,
+                                dtype=np.float64, diagnostics=diag)
+    border = diag["gamma_min_eig"] < BORDER["tensor"]
+    good = (ref64.temp_coh > 0.3) & ~border & np.all(np.isfinite(ref64.cpx_phase), axis=0)
+    assert good.mean() > 0.8
+    err = phase_err(out.cpx_phase[:, good], ref64.cpx_phase[:, good].astype(np.complex64))
+    assert err.max() < PHASE_TOL, err.max()
+    assert np.abs(out.temp_coh[good] - ref64.temp_coh[good]).max() < TC_TOL
+    np.testing.assert_array_equal(out.estimator[~border], ref64.estimator[~border])
