@@ -112,16 +112,19 @@ __global__ void __launch_bounds__(256) k_prep(const cfloat* __restrict__ slc, in
 // C (packed complex) | W1 (packed real) | S: staging for the window rows, or R (packed
 // complex) + W2 (packed real), or the full n x n LU of the fallback | v | d | piv
 struct PixLayout {
-    int n, np, stg;
-    size_t off_C, off_W1, off_S, off_W2, off_v, off_d, off_piv, bytes;
+    int n, np, stg, ldg;
+    size_t off_C, off_G, off_S, off_v, off_d, off_piv, bytes;
 };
 
-inline PixLayout make_layout(int n, int wx) {
+// C (packed complex) | G (n x ldg real) | S: staging for the covariance's window rows,
+// or R (packed complex), or the full n x n LU of the LU pass | v | d | piv
+inline PixLayout make_layout(int n, int wx, bool lu) {
     PixLayout L{};
     const size_t T = (size_t)n * (n + 1) / 2;
     L.n = n;
     L.np = (n + 1) & ~1;
     L.stg = wx * L.np + 32;
+    L.ldg = n | 1;
     size_t o = 0;
     auto take = [&](size_t bytes) {
         size_t at = o;
@@ -129,11 +132,10 @@ inline PixLayout make_layout(int n, int wx) {
         return at;
     };
     L.off_C = take(T * sizeof(cfloat));
-    L.off_W1 = take(T * sizeof(float));
-    const size_t rw2 = align_up(T * sizeof(cfloat), 16) + T * sizeof(float);
-    const size_t s_bytes = std::max({(size_t)L.stg * sizeof(cfloat), rw2, (size_t)n * n * sizeof(cfloat)});
+    L.off_G = take((size_t)n * L.ldg * sizeof(float));
+    size_t s_bytes = std::max((size_t)L.stg * sizeof(cfloat), T * sizeof(cfloat));
+    if (lu) s_bytes = std::max(s_bytes, (size_t)n * n * sizeof(cfloat));
     L.off_S = take(s_bytes);
-    L.off_W2 = L.off_S + align_up(T * sizeof(cfloat), 16);
     L.off_v = take(64 * sizeof(cfloat));
     L.off_d = take(64 * sizeof(float));
     L.off_piv = take(128 * sizeof(int));
@@ -146,8 +148,8 @@ enum PixMode { kCovOnly = 0, kSolveOnly = 1, kFused = 2 };
 struct PixArgs {
     int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
     int64_t npix;
-    int np, stg;
-    size_t off_C, off_W1, off_S, off_W2, off_v, off_d, off_piv, warp_bytes;
+    int np, stg, ldg;
+    size_t off_C, off_G, off_S, off_v, off_d, off_piv, warp_bytes;
     const cfloat* zt;        // (rows, cols, n) masked, pixel-major
     const uint8_t* nb_u8;    // (out_rows, out_cols, wy, wx) or null
     const uint32_t* nb_bits; // (out_rows, out_cols, wy, wpr) or null
@@ -166,6 +168,10 @@ struct PixArgs {
     float* tcoh;
     float* closure;          // (npix, n - 2) or null
     int32_t* counts;         // (npix) or null
+    int* fb_list;            // pixels whose EMI shifted matrix is indefinite (for the LU pass)
+    int* fb_count;
+    const int* list;         // LU pass: pixels list[0 .. *list_count)
+    const int* list_count;
 };
 
 }  // namespace dpl
@@ -260,21 +266,23 @@ __device__ void warp_covariance(const PixArgs& a, int64_t p, cfloat* C, cfloat* 
     if (count_out) *count_out = count;
 }
 
-template <int NB, int MODE>
+template <int NB, int MODE, bool kLU>
 __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
     extern __shared__ __align__(16) unsigned char pix_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     unsigned char* base = pix_smem + warp * a.warp_bytes;
     SolveMats m;
     m.C = reinterpret_cast<cfloat*>(base + a.off_C);
-    m.W1 = reinterpret_cast<float*>(base + a.off_W1);
+    m.G = reinterpret_cast<float*>(base + a.off_G);
+    m.ldg = a.ldg;
     m.R = reinterpret_cast<cfloat*>(base + a.off_S);
-    m.W2 = reinterpret_cast<float*>(base + a.off_W2);
     m.v = reinterpret_cast<cfloat*>(base + a.off_v);
     m.d = reinterpret_cast<float*>(base + a.off_d);
     m.piv = reinterpret_cast<int*>(base + a.off_piv);
     const int n = a.n;
-    for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
+    const int64_t total = kLU ? (int64_t)*a.list_count : a.npix;
+    for (int64_t idx = (int64_t)blockIdx.x * nwarps + warp; idx < total; idx += (int64_t)gridDim.x * nwarps) {
+        const int64_t p = kLU ? (int64_t)a.list[idx] : idx;
         if (MODE == kSolveOnly) {
             __syncwarp();
             if (a.Cplanar) {
@@ -302,7 +310,7 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
                 for (int j = lane; j < n; j += 32) dst[i * n + j] = cget(m.C, i, j);
             __syncwarp();
         } else {
-            solve_pixel<NB>(a, p, m, lane);
+            solve_pixel<NB, kLU>(a, p, m, lane);
         }
     }
 }
@@ -420,15 +428,15 @@ __global__ void __launch_bounds__(256) k_post(PostArgs a) {
 // ---------------------------------------------------------------------------------
 // host
 // ---------------------------------------------------------------------------------
-static void fill_pix_layout(PixArgs& a, int n, int wx) {
-    PixLayout L = make_layout(n, wx);
+static void fill_pix_layout(PixArgs& a, int n, int wx, bool lu = false) {
+    PixLayout L = make_layout(n, wx, lu);
     a.n = n;
     a.np = L.np;
     a.stg = L.stg;
+    a.ldg = L.ldg;
     a.off_C = L.off_C;
-    a.off_W1 = L.off_W1;
+    a.off_G = L.off_G;
     a.off_S = L.off_S;
-    a.off_W2 = L.off_W2;
     a.off_v = L.off_v;
     a.off_d = L.off_d;
     a.off_piv = L.off_piv;
@@ -444,8 +452,6 @@ struct PixTimer {
 };
 static PixTimer g_timer;
 
-template <int MODE>
-static dpl_status launch_pixel(PixArgs& a, cudaStream_t s);
 
 template <class F>
 static dpl_status timed(cudaStream_t s, int slot, F&& launch) {
@@ -464,9 +470,8 @@ static dpl_status timed(cudaStream_t s, int slot, F&& launch) {
     return st;
 }
 
-template <int MODE>
-static dpl_status launch_pixel(PixArgs& a, cudaStream_t s) {
-    if (a.npix == 0) return DPL_OK;
+template <int MODE, bool kLU>
+static dpl_status launch_pixel_pass(const PixArgs& a, cudaStream_t s) {
     // as many warps per CTA as fit ~100 KB (two CTAs per SM), at most 8
     int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)(100 * 1024) / a.warp_bytes));
     size_t smem = (size_t)warps * a.warp_bytes;
@@ -478,13 +483,32 @@ static dpl_status launch_pixel(PixArgs& a, cudaStream_t s) {
         DPL_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
         DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, warps * 32, smem));
-        int64_t want = (a.npix + warps - 1) / warps;
-        int64_t grid = std::min<int64_t>(want, (int64_t)std::max(1, per_sm) * std::max(1, sms) * 8);
-        kernel<<<(unsigned)grid, warps * 32, smem, s>>>(a);
-        return check_launch("k_pixel");
+        const int64_t resident = (int64_t)std::max(1, per_sm) * std::max(1, sms);
+        int64_t grid = kLU ? resident : std::min<int64_t>((a.npix + warps - 1) / warps, resident * 8);
+        kernel<<<(unsigned)std::max<int64_t>(grid, 1), warps * 32, smem, s>>>(a);
+        return check_launch(kLU ? "k_pixel (LU pass)" : "k_pixel");
     };
-    if (a.n <= 32) return go(k_pixel<1, MODE>);
-    return go(k_pixel<2, MODE>);
+    if (a.n <= 32) return go(k_pixel<1, MODE, kLU>);
+    return go(k_pixel<2, MODE, kLU>);
+}
+
+// Main pass (Cholesky inverse iteration) and, for the pixels it lists, the LU pass.
+// `fb` holds a counter followed by room for every pixel index.
+template <int MODE>
+static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr) {
+    if (a.npix == 0) return DPL_OK;
+    if (MODE == kCovOnly) return launch_pixel_pass<MODE, false>(a, s);
+    if (!fb) return fail(DPL_ERR_WORKSPACE, "solver: missing fallback list");
+    DPL_CUDA_TRY(cudaMemsetAsync(fb, 0, sizeof(int), s));
+    a.fb_count = fb;
+    a.fb_list = fb + 64;
+    dpl_status st = launch_pixel_pass<MODE, false>(a, s);
+    if (st != DPL_OK) return st;
+    PixArgs b = a;
+    fill_pix_layout(b, a.n, 2 * a.hx + 1, true);
+    b.list = a.fb_list;
+    b.list_count = a.fb_count;
+    return launch_pixel_pass<MODE, true>(b, s);
 }
 
 // Tensor-core covariance: fills `Cg` (npix x n*n planar floats).
@@ -574,6 +598,7 @@ struct PlWorkspace {
     int* status;
     unsigned int* valid_bits;
     float* Cg;
+    int* fb;
     uint8_t* flags;
     float* avgmag;
     cfloat* zt;
@@ -589,6 +614,7 @@ static size_t pl_workspace_layout(int64_t n, int64_t rows, int64_t cols, int sy,
     t.status = ws.take<int>(16);
     t.valid_bits = ws.take<unsigned int>(16);
     t.Cg = cov_form == 0 ? ws.take<float>(P * n * n) : nullptr;
+    t.fb = ws.take<int>(P + 64);
     t.flags = ws.take<uint8_t>(npix);
     t.avgmag = ws.take<float>(npix);
     t.zt = ws.take<cfloat>(npix * n);
@@ -681,10 +707,10 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
             });
             if (st != DPL_OK) return st;
             a.Cplanar = w.Cg;
-            st = timed(s, 1, [&] { return launch_pixel<kSolveOnly>(a, s); });
+            st = timed(s, 1, [&] { return launch_pixel<kSolveOnly>(a, s, w.fb); });
         } else {
             // plain form: SIMT covariance fused with the solver
-            st = timed(s, 0, [&] { return launch_pixel<kFused>(a, s); });
+            st = timed(s, 0, [&] { return launch_pixel<kFused>(a, s, w.fb); });
         }
         if (st != DPL_OK) return st;
 
@@ -791,8 +817,7 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
 }
 
 extern "C" size_t dpl_process_coherence_workspace_size(int64_t npix) {
-    (void)npix;
-    return 256;
+    return align_up((size_t)(std::max<int64_t>(npix, 0) + 64) * sizeof(int), 256);
 }
 
 extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use_evd, double beta,
@@ -819,9 +844,9 @@ extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int ns
     a.crlb = crlb_std_dev;
     a.tcoh = temp_coh;
     a.closure = nslc > 2 ? closure_phases : nullptr;
-    (void)workspace;
-    (void)workspace_bytes;
-    return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream);
+    if (!workspace || workspace_bytes < dpl_process_coherence_workspace_size(npix))
+        return fail(DPL_ERR_WORKSPACE, "dpl_process_coherence: workspace too small");
+    return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream, reinterpret_cast<int*>(workspace));
 }
 
 extern "C" dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches) {

@@ -1,25 +1,28 @@
 // Per-pixel solver: one warp per pixel, matrices in the warp's shared memory.
 //
-// Storage is packed lower-triangular (element (i, j), j <= i, at i(i+1)/2 + j): the
-// coherence matrix C and every matrix derived from it is Hermitian or symmetric,
-// so this halves shared memory per warp and lets more warps share an SM.  Loops
-// run over rows with the lanes over columns (no index division, short divergent
-// tails); triangular solves keep the iterate in registers (lane i owns entry i,
-// entry i + 32 for N > 32) and broadcast pivots with shuffles.
+// Storage: the coherence matrix C and the EMI factor R are packed lower-triangular
+// complex (element (i, j), j <= i, at i(i+1)/2 + j); the real |Gamma| work matrix G
+// is full with an odd row stride (conflict-free column access).  Loops run over rows
+// with the lanes over columns; triangular solves keep the iterate in registers
+// (lane i owns entry i, and entry i + 32 when N > 32) and broadcast with shuffles.
 //
 // Algorithms (all float32, as the reference):
-//   |Gamma| (+ beta I, zero threshold) + 1e-6 I = L L^T     (_core.py:452-467)
-//   Y = L^{-1} (row by row), |Gamma|^{-1} = Y^T Y            (cho_solve(I), :472)
+//   |Gamma| (+ beta I, zero threshold) + 1e-6 I, inverted in place by Gauss-Jordan
+//        elimination (the symmetric positive definite case needs no pivoting; a
+//        non-positive pivot means "not positive definite", where the reference's
+//        cho_factor fails and the pixel falls back to EVD)      (_core.py:452-515)
 //   EMI: A - 0.99 I = R R^H (complex Cholesky of the Hermitian shifted matrix) and
 //        inverse iteration v <- (R R^H)^{-1} v / |.|, <= 49 steps, stop at
 //        |v_new - v| <= 1e-5 (_eigenvalues.py:139-205).  These are the iterates of
-//        the reference's LU solve; where A - 0.99 I is not positive definite the
-//        same iteration runs on an LU factorisation with partial pivoting.
+//        the reference's LU solve.  Where A - 0.99 I is not positive definite the
+//        pixel is listed and a second pass runs the same iteration on an LU
+//        factorisation with partial pivoting (the reference's algorithm).
 //        lambda = v^H A v = |R^H v|^2 + 0.99 |v|^2.
 //   EVD: power iteration on C o |C| (_eigenvalues.py:93-136) for use_evd and for
-//        pixels whose |Gamma|^{-1} has NaNs (_core.py:496-515).
-//   CRLB: FIM = 2L (Gamma o Gamma^{-1} - I) without row/column `ref`, + 1e-6 I,
-//        sigma = sqrt(diag FIM^{-1}) with 0 at `ref` (crlb.py:132-189).
+//        pixels whose |Gamma|^{-1} has NaNs.
+//   CRLB: FIM = 2L (Gamma o Gamma^{-1} - I) with row/column `ref` replaced by the
+//        identity, + 1e-6 I, inverted by Gauss-Jordan; sigma = sqrt(diag FIM^{-1}),
+//        0 at `ref` (crlb.py:132-189).
 #pragma once
 
 namespace dpl {
@@ -34,77 +37,94 @@ __device__ __forceinline__ cfloat cget(const cfloat* C, int i, int j) {
 
 struct SolveMats {
     cfloat* C;   // packed coherence
-    float* W1;   // packed real
-    float* W2;   // packed real
-    cfloat* R;   // packed complex factor / B for EVD; LU (full, ld = n) on the fallback
+    float* G;    // n x ldg real work matrix
+    int ldg;
+    cfloat* R;   // packed complex (EMI factor, or C o |C| for EVD); full n x n LU in the LU pass
     cfloat* v;   // 64 published vector entries
-    float* d;    // 64 floats
-    int* piv;    // 64 pivots (LU fallback)
+    float* d;    // 64 floats (inverse diagonal of R)
+    int* piv;    // 128 ints (LU pass)
 };
 
-// Real Cholesky in place on packed W (n x n).  Uniform result.
-__device__ bool s_chol_real(float* W, int n, int lane) {
+// unit phasor exp(i angle(c)) via rsqrt; angle(+0) = 0, angle(-0 + 0j) = pi
+__device__ __forceinline__ cfloat fphasor(cfloat c) {
+    const float m2 = c.re * c.re + c.im * c.im;
+    if (m2 == 0.f) return cmake(signbit(c.re) ? -1.f : 1.f, 0.f);
+    if (!(m2 <= INFINITY)) return cmake(nanf(""), nanf(""));
+    const float r = rsqrtf(m2);
+    return cmake(c.re * r, c.im * r);
+}
+
+// In-place inverse of a symmetric positive definite n x n matrix by Gauss-Jordan
+// elimination.  Returns false (uniformly) on a non-positive pivot.  Lanes own
+// columns; column k is left unchanged by the row sweep (its multiplier is 0) and
+// rewritten afterwards.
+template <int NB>
+__device__ bool s_gauss_jordan_spd(float* A, int n, int ld, int lane) {
     for (int k = 0; k < n; ++k) {
         __syncwarp();
-        const float d = W[pk(k, k)];
-        if (!(d > 0.f)) return false;
-        const float lkk = fsqrt(d);
-        __syncwarp();
-        for (int i = k + 1 + lane; i < n; i += 32) W[pk(i, k)] = fdiv(W[pk(i, k)], lkk);
-        if (lane == 0) W[pk(k, k)] = lkk;
-        __syncwarp();
+        const float piv = A[k * ld + k];
+        if (!(piv > 0.f)) return false;
+        const float inv = 1.f / piv;
+        float rk[NB], rm[NB];
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int j = lane + 32 * q;
+            rk[q] = j < n ? (j == k ? inv : A[k * ld + j] * inv) : 0.f;
+            rm[q] = j == k ? 0.f : rk[q];
+        }
+        const float* colk = A + k;
+        float* mine = A + lane;
+#pragma unroll 4
+        for (int i = 0; i < k; ++i) {
+            const float f = colk[i * ld];
+#pragma unroll
+            for (int q = 0; q < NB; ++q)
+                if (lane + 32 * q < n) mine[i * ld + 32 * q] -= f * rm[q];
+        }
+#pragma unroll 4
         for (int i = k + 1; i < n; ++i) {
-            const float lik = W[pk(i, k)];
-            for (int j = k + 1 + lane; j <= i; j += 32) W[pk(i, j)] -= lik * W[pk(j, k)];
+            const float f = colk[i * ld];
+#pragma unroll
+            for (int q = 0; q < NB; ++q)
+                if (lane + 32 * q < n) mine[i * ld + 32 * q] -= f * rm[q];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int i = lane + 32 * q;
+            if (i < n && i != k) A[i * ld + k] = -A[i * ld + k] * inv;
+            if (i < n) A[k * ld + i] = rk[q];
         }
     }
     __syncwarp();
     return true;
 }
 
-// Y = L^{-1} (packed, lower) from packed L: row i = (e_i - sum_{k<i} l_ik y_k) / l_ii.
-// If sumsq != nullptr, also the column sums of squares sum_k Y_kj^2 (lane-owned j).
-__device__ void s_tri_inverse(const float* L, float* Y, int n, int lane, float* sumsq) {
-    for (int i = 0; i < n; ++i) {
-        __syncwarp();
-        const float lii = L[pk(i, i)];
-        for (int j = lane; j <= i; j += 32) {
-            float s = i == j ? 1.f : 0.f;
-            for (int k = j; k < i; ++k) s -= L[pk(i, k)] * Y[pk(k, j)];
-            Y[pk(i, j)] = fdiv(s, lii);
-        }
-    }
-    __syncwarp();
-    if (sumsq) {
-        for (int j = lane; j < n; j += 32) {
-            float ss = 0.f;
-            for (int k = j; k < n; ++k) {
-                const float y = Y[pk(k, j)];
-                ss += y * y;
-            }
-            sumsq[j] = ss;
-        }
-        __syncwarp();
-    }
-}
-
-// Complex Cholesky in place on packed R (Hermitian, lower stored).  Uniform result.
-__device__ bool s_chol_complex(cfloat* R, int n, int lane) {
+// Complex Cholesky in place on packed R (Hermitian, lower stored); dinv[k] = 1/R_kk.
+__device__ bool s_chol_complex(cfloat* R, float* dinv, int n, int lane) {
     for (int k = 0; k < n; ++k) {
         __syncwarp();
         const float d = R[pk(k, k)].re;
         if (!(d > 0.f)) return false;
-        const float lkk = fsqrt(d);
+        const float lkk = sqrtf(d);
+        const float il = 1.f / lkk;
+        for (int i = k + 1 + lane; i < n; i += 32) R[pk(i, k)] = cscale(R[pk(i, k)], il);
         __syncwarp();
-        for (int i = k + 1 + lane; i < n; i += 32) {
-            const cfloat x = R[pk(i, k)];
-            R[pk(i, k)] = cmake(fdiv(x.re, lkk), fdiv(x.im, lkk));
+        if (lane == 0) {
+            R[pk(k, k)] = cmake(lkk, 0.f);
+            dinv[k] = il;
         }
-        if (lane == 0) R[pk(k, k)] = cmake(lkk, 0.f);
-        __syncwarp();
+        // trailing update R_ij -= R_ik conj(R_jk), k < j <= i; lanes own columns j
+        const int j0 = k + 1 + lane, j1 = j0 + 32;
+        const cfloat l0 = j0 < n ? R[pk(j0, k)] : cmake(0.f, 0.f);
+        const cfloat l1 = j1 < n ? R[pk(j1, k)] : cmake(0.f, 0.f);
+        int bi = tri(k + 1);
+#pragma unroll 2
         for (int i = k + 1; i < n; ++i) {
-            const cfloat lik = R[pk(i, k)];
-            for (int j = k + 1 + lane; j <= i; j += 32) R[pk(i, j)] = csub(R[pk(i, j)], cmulc(lik, R[pk(j, k)]));
+            const cfloat lik = R[bi + k];
+            if (j0 <= i) R[bi + j0] = csub(R[bi + j0], cmulc(lik, l0));
+            if (j1 <= i) R[bi + j1] = csub(R[bi + j1], cmulc(lik, l1));
+            bi += i + 1;
         }
     }
     __syncwarp();
@@ -129,31 +149,35 @@ __device__ __forceinline__ float s_norm2(const cfloat (&x)[NB]) {
     return warp_sum(s);
 }
 
-// x <- (R R^H)^{-1} x with packed lower R (real positive diagonal)
+// x <- (R R^H)^{-1} x with packed lower R and dinv = 1 / diag(R)
 template <int NB>
-__device__ void s_chol_solve(const cfloat* R, int n, cfloat (&x)[NB], int lane) {
+__device__ void s_chol_solve(const cfloat* R, const float* dinv, int n, cfloat (&x)[NB], int lane) {
+    int base[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) base[q] = tri(lane + 32 * q);
     for (int k = 0; k < n; ++k) {
-        const float rkk = R[pk(k, k)].re;
+        const float dk = dinv[k];
 #pragma unroll
         for (int q = 0; q < NB; ++q)
-            if (lane + 32 * q == k) x[q] = cmake(fdiv(x[q].re, rkk), fdiv(x[q].im, rkk));
+            if (lane + 32 * q == k) x[q] = cscale(x[q], dk);
         const cfloat yk = s_bcast<NB>(x, k);
 #pragma unroll
         for (int q = 0; q < NB; ++q) {
             const int i = lane + 32 * q;
-            if (i > k && i < n) x[q] = csub(x[q], cmul(R[pk(i, k)], yk));
+            if (i > k && i < n) x[q] = csub(x[q], cmul(R[base[q] + k], yk));
         }
     }
     for (int k = n - 1; k >= 0; --k) {
-        const float rkk = R[pk(k, k)].re;
+        const float dk = dinv[k];
 #pragma unroll
         for (int q = 0; q < NB; ++q)
-            if (lane + 32 * q == k) x[q] = cmake(fdiv(x[q].re, rkk), fdiv(x[q].im, rkk));
+            if (lane + 32 * q == k) x[q] = cscale(x[q], dk);
         const cfloat xk = s_bcast<NB>(x, k);
+        const int bk = tri(k);
 #pragma unroll
         for (int q = 0; q < NB; ++q) {
             const int i = lane + 32 * q;
-            if (i < k) x[q] = csub(x[q], cmul(cconj(R[pk(k, i)]), xk));
+            if (i < k) x[q] = csub(x[q], cmul(cconj(R[bk + i]), xk));
         }
     }
 }
@@ -241,12 +265,12 @@ __device__ void s_lu_solve(const cfloat* A, int n, const int* src, cfloat (&x)[N
 }
 
 __device__ __forceinline__ float s_gamma(const PixArgs& a, cfloat c, bool diag) {
-    float g = hypotf(c.re, c.im);
+    float g = sqrtf(c.re * c.re + c.im * c.im);
     if (a.beta_on) g = fadd(fmul(a.one_minus_beta, g), diag ? a.beta : 0.f);
     return g < a.zct ? 0.f : g;
 }
 
-// y_i = sum_j H_ij x_j for Hermitian H in packed lower storage; x published in vpub
+// y = H x for Hermitian H in packed lower storage; x published in vpub
 template <int NB>
 __device__ void s_hermv(const cfloat* H, int n, const cfloat* vpub, cfloat (&y)[NB], int lane) {
 #pragma unroll
@@ -254,7 +278,9 @@ __device__ void s_hermv(const cfloat* H, int n, const cfloat* vpub, cfloat (&y)[
         const int i = lane + 32 * q;
         cfloat acc = cmake(0.f, 0.f);
         if (i < n) {
-            for (int j = 0; j < n; ++j) acc = cadd(acc, cmul(cget(H, i, j), vpub[j]));
+            const int bi = tri(i);
+            for (int j = 0; j <= i; ++j) acc = cadd(acc, cmul(H[bi + j], vpub[j]));
+            for (int j = i + 1; j < n; ++j) acc = cadd(acc, cmul(cconj(H[tri(j) + i]), vpub[j]));
         }
         y[q] = acc;
     }
@@ -269,11 +295,36 @@ __device__ void s_publish(cfloat* vpub, const cfloat (&x)[NB], int n, int lane) 
     __syncwarp();
 }
 
-// Full solve for one pixel whose packed coherence matrix is in m.C.
-template <int NB>
+// Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps.
+template <int NB, class Op>
+__device__ void s_iterate(cfloat (&v)[NB], Op&& op) {
+    float diff = 1.f;
+    for (int it = 1; diff > 1e-5f && it < 50; ++it) {
+        cfloat x[NB];
+#pragma unroll
+        for (int q = 0; q < NB; ++q) x[q] = v[q];
+        op(x);
+        const float nrm = sqrtf(s_norm2<NB>(x));
+        const float inv = 1.f / nrm;
+        float dd = 0.f;
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            x[q] = cscale(x[q], inv);
+            dd += cabs2(csub(x[q], v[q]));
+            v[q] = x[q];
+        }
+        diff = sqrtf(warp_sum(dd));
+    }
+}
+
+// Full solve for one pixel whose packed coherence matrix is in m.C.  With kLU the
+// EMI step uses LU with partial pivoting; otherwise a pixel whose shifted matrix is
+// not positive definite is appended to a.fb_list and left for the LU pass.
+template <int NB, bool kLU>
 __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int lane) {
-    const int n = a.n, T = tri(n);
+    const int n = a.n, ld = m.ldg;
     cfloat* C = m.C;
+    float* G = m.G;
     if (a.baseline_lag > 0) {
         for (int i = a.baseline_lag; i < n; ++i)
             for (int j = lane; j <= i - a.baseline_lag; j += 32) C[pk(i, j)] = cmake(0.f, 0.f);
@@ -285,89 +336,66 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
             a.closure[p * (n - 2) + i] = atan2f(c.im, c.re);
         }
     }
-    // |Gamma| + 1e-6 I -> L (W1) -> Y (W2) -> |Gamma|^{-1} (W1)
+    // |Gamma| + 1e-6 I (full) -> |Gamma|^{-1}
     for (int i = 0; i < n; ++i)
-        for (int j = lane; j <= i; j += 32) m.W1[pk(i, j)] = fadd(s_gamma(a, C[pk(i, j)], i == j), i == j ? 1e-6f : 0.f);
-    bool inv_nan;
-    if (s_chol_real(m.W1, n, lane)) {
-        s_tri_inverse(m.W1, m.W2, n, lane, nullptr);
-        bool bad = false;
-        for (int i = 0; i < n; ++i) {
-            for (int j = lane; j <= i; j += 32) {
-                float s = 0.f;
-                for (int k = i; k < n; ++k) s += m.W2[pk(k, i)] * m.W2[pk(k, j)];
-                m.W1[pk(i, j)] = s;
-                bad |= isnan(s);
-            }
+        for (int j = lane; j < n; j += 32) {
+            const int r = j <= i ? i : j, c = j <= i ? j : i;
+            G[i * ld + j] = fadd(s_gamma(a, C[pk(r, c)], i == j), i == j ? 1e-6f : 0.f);
         }
+    bool inv_nan;
+    if (s_gauss_jordan_spd<NB>(G, n, ld, lane)) {
+        bool bad = false;
+        for (int i = 0; i < n; ++i)
+            for (int j = lane; j < n; j += 32) bad |= isnan(G[i * ld + j]);
         inv_nan = warp_any(bad);
     } else {
-        for (int e = lane; e < T; e += 32) m.W1[e] = nanf("");
+        __syncwarp();
+        for (int i = 0; i < n; ++i)
+            for (int j = lane; j < n; j += 32) G[i * ld + j] = nanf("");
         inv_nan = true;
     }
     __syncwarp();
     const bool evd = a.use_evd || inv_nan;
-    // A - 0.99 I (EMI) or C o |C| (EVD) into R
-    if (!evd) {
-        for (int i = 0; i < n; ++i)
-            for (int j = lane; j <= i; j += 32) {
-                cfloat x = cscale(C[pk(i, j)], m.W1[pk(i, j)]);
-                if (i == j) x.re = fsub(x.re, 0.99f);
-                m.R[pk(i, j)] = x;
-            }
-    } else {
-        for (int e = lane; e < T; e += 32) {
-            const cfloat c = C[e];
-            m.R[e] = cscale(c, hypotf(c.re, c.im));
-        }
-    }
-    __syncwarp();
+
     cfloat v[NB];
-    const float inv_sqrt_n = fdiv(1.f, fsqrt((float)n));
+    const float inv_sqrt_n = 1.f / sqrtf((float)n);
 #pragma unroll
     for (int q = 0; q < NB; ++q) v[q] = lane + 32 * q < n ? cmake(inv_sqrt_n, 0.f) : cmake(0.f, 0.f);
     float lambda;
     if (!evd) {
-        // keep A - 0.99 I (full) for the LU fallback before factorising in place
-        const bool chol_ok = s_chol_complex(m.R, n, lane);
-        if (chol_ok) {
-            float diff = 1.f;
-            for (int it = 1; diff > 1e-5f && it < 50; ++it) {
-                cfloat x[NB];
-#pragma unroll
-                for (int q = 0; q < NB; ++q) x[q] = v[q];
-                s_chol_solve<NB>(m.R, n, x, lane);
-                const float nrm = fsqrt(s_norm2<NB>(x));
-                float dd = 0.f;
-#pragma unroll
-                for (int q = 0; q < NB; ++q) {
-                    x[q] = cmake(fdiv(x[q].re, nrm), fdiv(x[q].im, nrm));
-                    dd += cabs2(csub(x[q], v[q]));
-                    v[q] = x[q];
+        if (!kLU) {
+            // packed A - 0.99 I, complex Cholesky, inverse iteration
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j <= i; j += 32) {
+                    cfloat x = cscale(C[pk(i, j)], G[i * ld + j]);
+                    if (i == j) x.re = fsub(x.re, 0.99f);
+                    m.R[pk(i, j)] = x;
                 }
-                diff = fsqrt(warp_sum(dd));
+            __syncwarp();
+            if (!s_chol_complex(m.R, m.d, n, lane)) {
+                if (lane == 0) a.fb_list[atomicAdd(a.fb_count, 1)] = (int)p;
+                __syncwarp();
+                return;
             }
-            // lambda = |R^H v|^2 + 0.99 |v|^2
+            s_iterate<NB>(v, [&](cfloat(&x)[NB]) { s_chol_solve<NB>(m.R, m.d, n, x, lane); });
             s_publish<NB>(m.v, v, n, lane);
             float s = 0.f;
 #pragma unroll
             for (int q = 0; q < NB; ++q) {
                 const int i = lane + 32 * q;
                 if (i < n) {
-                    cfloat acc = cmake(0.f, 0.f);
+                    cfloat acc = cmake(0.f, 0.f);  // (R^H v)_i = sum_{k >= i} conj(R_ki) v_k
                     for (int k = i; k < n; ++k) acc = cadd(acc, cmulc(m.v[k], m.R[pk(k, i)]));
                     s += cabs2(acc);
                 }
             }
             lambda = fadd(warp_sum(s), fmul(0.99f, s_norm2<NB>(v)));
         } else {
-            // LU fallback on the full shifted matrix (rebuilt from C and |Gamma|^{-1})
-            cfloat* A = m.R;  // the scratch region holds n*n complex (see the layout)
-            __syncwarp();
+            // LU with partial pivoting on the full shifted matrix
+            cfloat* A = m.R;
             for (int i = 0; i < n; ++i)
                 for (int j = lane; j < n; j += 32) {
-                    const cfloat c = cget(C, i, j);
-                    cfloat x = cscale(c, j <= i ? m.W1[pk(i, j)] : m.W1[pk(j, i)]);
+                    cfloat x = cscale(cget(C, i, j), G[i * ld + j]);
                     if (i == j) x.re = fsub(x.re, 0.99f);
                     A[i * n + j] = x;
                 }
@@ -384,23 +412,7 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
                 }
             }
             __syncwarp();
-            float diff = 1.f;
-            for (int it = 1; diff > 1e-5f && it < 50; ++it) {
-                cfloat x[NB];
-#pragma unroll
-                for (int q = 0; q < NB; ++q) x[q] = v[q];
-                s_lu_solve<NB>(A, n, src, x, lane);
-                const float nrm = fsqrt(s_norm2<NB>(x));
-                float dd = 0.f;
-#pragma unroll
-                for (int q = 0; q < NB; ++q) {
-                    x[q] = cmake(fdiv(x[q].re, nrm), fdiv(x[q].im, nrm));
-                    dd += cabs2(csub(x[q], v[q]));
-                    v[q] = x[q];
-                }
-                diff = fsqrt(warp_sum(dd));
-            }
-            // lambda = Re(v^H (|Gamma|^{-1} o C) v)
+            s_iterate<NB>(v, [&](cfloat(&x)[NB]) { s_lu_solve<NB>(A, n, src, x, lane); });
             s_publish<NB>(m.v, v, n, lane);
             float s = 0.f;
 #pragma unroll
@@ -408,34 +420,26 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
                 const int i = lane + 32 * q;
                 if (i < n) {
                     cfloat acc = cmake(0.f, 0.f);
-                    for (int j = 0; j < n; ++j) {
-                        const float w = j <= i ? m.W1[pk(i, j)] : m.W1[pk(j, i)];
-                        acc = cadd(acc, cmul(cscale(cget(C, i, j), w), m.v[j]));
-                    }
+                    for (int j = 0; j < n; ++j) acc = cadd(acc, cmul(cscale(cget(C, i, j), G[i * ld + j]), m.v[j]));
                     s += v[q].re * acc.re + v[q].im * acc.im;
                 }
             }
             lambda = warp_sum(s);
         }
-        const float scale = fdiv(fsqrt((float)n), fsqrt(s_norm2<NB>(v)));
+        const float scale = sqrtf((float)n) / sqrtf(s_norm2<NB>(v));
 #pragma unroll
         for (int q = 0; q < NB; ++q) v[q] = cscale(v[q], scale);
     } else {
-        float diff = 1.f;
-        for (int it = 1; diff > 1e-5f && it < 50; ++it) {
-            s_publish<NB>(m.v, v, n, lane);
-            cfloat y[NB];
-            s_hermv<NB>(m.R, n, m.v, y, lane);
-            const float nrm = fsqrt(s_norm2<NB>(y));
-            float dd = 0.f;
-#pragma unroll
-            for (int q = 0; q < NB; ++q) {
-                y[q] = cmake(fdiv(y[q].re, nrm), fdiv(y[q].im, nrm));
-                dd += cabs2(csub(y[q], v[q]));
-                v[q] = y[q];
-            }
-            diff = fsqrt(warp_sum(dd));
+        const int T = tri(n);
+        for (int e = lane; e < T; e += 32) {
+            const cfloat c = C[e];
+            m.R[e] = cscale(c, sqrtf(c.re * c.re + c.im * c.im));
         }
+        __syncwarp();
+        s_iterate<NB>(v, [&](cfloat(&x)[NB]) {
+            s_publish<NB>(m.v, x, n, lane);
+            s_hermv<NB>(m.R, n, m.v, x, lane);
+        });
         s_publish<NB>(m.v, v, n, lane);
         cfloat y[NB];
         s_hermv<NB>(m.R, n, m.v, y, lane);
@@ -445,31 +449,30 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
         lambda = warp_sum(s);
     }
     __syncwarp();
-    // CRLB (needs |Gamma|^{-1} in W1; FIM in W2, its inverse factor in the R region)
+    // CRLB: FIM in place of |Gamma|^{-1} (row/col `ref` -> identity), Gauss-Jordan
     if (a.compute_crlb) {
         const int ref = a.crlb_ref;
         for (int i = 0; i < n; ++i)
-            for (int j = lane; j <= i; j += 32) {
+            for (int j = lane; j < n; j += 32) {
                 float f;
                 if (i == ref || j == ref) {
                     f = i == j ? 1.f : 0.f;
                 } else {
+                    const int r = j <= i ? i : j, c = j <= i ? j : i;
                     const float x = fmul(a.crlb_factor,
-                                         fsub(fmul(s_gamma(a, C[pk(i, j)], i == j), m.W1[pk(i, j)]), i == j ? 1.f : 0.f));
+                                         fsub(fmul(s_gamma(a, C[pk(r, c)], i == j), G[i * ld + j]), i == j ? 1.f : 0.f));
                     f = i == j ? fadd(x, 1e-6f) : x;
                 }
-                m.W2[pk(i, j)] = f;
+                G[i * ld + j] = f;
             }
-        const bool ok = s_chol_real(m.W2, n, lane);
-        if (ok) s_tri_inverse(m.W2, reinterpret_cast<float*>(m.R), n, lane, m.d);
-        for (int t = lane; t < n; t += 32) a.crlb[p * n + t] = t == ref ? 0.f : (ok ? fsqrt(m.d[t]) : nanf(""));
+        const bool ok = s_gauss_jordan_spd<NB>(G, n, ld, lane);
+        for (int t = lane; t < n; t += 32) a.crlb[p * n + t] = t == ref ? 0.f : (ok ? sqrtf(G[t * ld + t]) : nanf(""));
         __syncwarp();
     } else {
         for (int t = lane; t < n; t += 32) a.crlb[p * n + t] = 0.f;
     }
-
     // reference to reference_idx
-    const cfloat rot = cconj(cphasor(s_bcast<NB>(v, a.ref_idx)));
+    const cfloat rot = cconj(fphasor(s_bcast<NB>(v, a.ref_idx)));
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
         const int i = lane + 32 * q;
@@ -480,16 +483,20 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
         a.eig[p] = lambda;
         a.est[p] = evd ? 0 : 1;
     }
-    s_publish<NB>(m.v, v, n, lane);
-    // temporal coherence over pairs i < j (stored as packed (j, i))
+    // temporal coherence over pairs i < j: phasor(C_ij) conj(phasor(v_i conj v_j)),
+    // with C_ij = conj(C_ji) (packed (j, i)) and phasor(v_i conj v_j) = w_i conj(w_j)
+    cfloat w[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) w[q] = fphasor(v[q]);
+    s_publish<NB>(m.v, w, n, lane);
     float sre = 0.f, sim = 0.f;
     int cnt = 0;
     for (int r = 1; r < n; ++r) {
-        const cfloat vr = m.v[r];
+        const cfloat wr = m.v[r];
+        const int br = tri(r);
         for (int c = lane; c < r; c += 32) {
-            const cfloat u = cphasor(cconj(C[pk(r, c)]));    // phasor of C_cr
-            const cfloat w = cphasor(cmulc(m.v[c], vr));     // v_c conj(v_r)
-            const cfloat t = cmulc(u, w);
+            const cfloat u = fphasor(C[br + c]);                   // phasor of C_rc = conj phasor of C_cr
+            const cfloat t = cconj(cmulc(cmul(u, m.v[c]), wr));   // conj(u_rc w_c conj(w_r))
             if (!cisnan(t)) {
                 sre += t.re;
                 sim += t.im;
@@ -502,7 +509,7 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
     cnt = warp_sum_int(cnt);
     if (lane == 0) {
         const float fc = (float)cnt;
-        const float tc = hypotf(fdiv(sre, fc), fdiv(sim, fc));
+        const float tc = hypotf(sre / fc, sim / fc);
         a.tcoh[p] = isfinite(tc) ? tc : 0.f;
     }
     __syncwarp();
