@@ -20,6 +20,7 @@
 // Precision: float32 throughout, as in the reference (jax with x64 disabled).
 // Iteration caps and tolerances are the reference's (<= 49 iterations, 1e-5).
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <sstream>
@@ -847,6 +848,66 @@ extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int ns
     if (!workspace || workspace_bytes < dpl_process_coherence_workspace_size(npix))
         return fail(DPL_ERR_WORKSPACE, "dpl_process_coherence: workspace too small");
     return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream, reinterpret_cast<int*>(workspace));
+}
+
+// Scratch of dpl_process_coherence_noalloc: the fallback-pixel counter (word 0) and
+// list (from word 64) of launch_pixel, sized for kNoAllocMaxPix pixels (4 MiB).  One
+// copy per device, shared by every call on that device.
+constexpr int64_t kNoAllocMaxPix = int64_t(1) << 20;
+static __device__ __align__(256) int g_noalloc_scratch[64 + kNoAllocMaxPix];
+
+static std::mutex g_noalloc_mu;
+static int* g_noalloc_ptr[64];  // per device ordinal, resolved on the first call there
+
+extern "C" int64_t dpl_process_coherence_noalloc_max_pixels(void) { return kNoAllocMaxPix; }
+
+extern "C" dpl_status dpl_process_coherence_noalloc(const float* C, int64_t npix, int nslc, int use_evd,
+                                                    double beta, double zero_correlation_threshold,
+                                                    int reference_idx, double num_looks, int first_real_slc_idx,
+                                                    int compute_crlb, float* eig_vecs, float* eig_vals,
+                                                    uint8_t* estimator, float* crlb_std_dev, float* temp_coh,
+                                                    float* closure_phases, dpl_stream_t stream) {
+    if (npix < 0 || nslc <= 0) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_noalloc: bad shape");
+    if (npix > kNoAllocMaxPix) {
+        char msg[160];
+        snprintf(msg, sizeof msg,
+                 "dpl_process_coherence_noalloc: npix=%lld exceeds the static scratch limit of %lld pixels",
+                 (long long)npix, (long long)kNoAllocMaxPix);
+        return fail(DPL_ERR_UNSUPPORTED, msg);
+    }
+    if (nslc > kMaxNslc) return fail(DPL_ERR_UNSUPPORTED, "at most 64 SLCs per call are supported");
+    if (npix == 0) return DPL_OK;
+    if (!C || !eig_vecs || !eig_vals || !estimator || !crlb_std_dev || !temp_coh)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_noalloc: null pointer");
+    const int ref = norm_ref(reference_idx, nslc);
+    if (ref < 0 || ref >= nslc) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
+    int dev = 0;
+    DPL_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(DPL_ERR_UNSUPPORTED, "dpl_process_coherence_noalloc: device ordinal >= 64");
+    int* scratch = nullptr;
+    {
+        // set-up on the first call on this device (the current one): the symbol's address
+        std::lock_guard<std::mutex> g(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            DPL_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            g_noalloc_ptr[dev] = static_cast<int*>(p);
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    PixArgs a{};
+    fill_pix_layout(a, nslc, 1);
+    a.npix = npix;
+    a.Cin = reinterpret_cast<const cfloat*>(C);
+    set_solver_params(a, use_evd, beta, zero_correlation_threshold, ref, num_looks, first_real_slc_idx, compute_crlb);
+    a.vout = reinterpret_cast<cfloat*>(eig_vecs);
+    a.eig = eig_vals;
+    a.est = estimator;
+    a.crlb = crlb_std_dev;
+    a.tcoh = temp_coh;
+    a.closure = nslc > 2 ? closure_phases : nullptr;
+    // launch_pixel zeroes the counter on the stream before the solve; the list needs no clearing
+    return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream, scratch);
 }
 
 extern "C" dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches) {

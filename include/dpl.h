@@ -168,6 +168,29 @@ dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use
                                  float* crlb_std_dev, float* temp_coh, float* closure_phases,
                                  void* workspace, size_t workspace_bytes, dpl_stream_t stream);
 
+/* No counterpart in the reference: dpl_process_coherence without a caller-supplied
+ * workspace, for callers that cannot allocate device memory per call (a C/GDAL-style
+ * host that owns no device allocator and cannot size one, or a multi-stream pipeline
+ * where cudaMalloc/cudaFree would synchronise the device).  Same arguments, meaning
+ * and results as dpl_process_coherence; allocates nothing.
+ * Scratch: a static device array of 64 + dpl_process_coherence_noalloc_max_pixels()
+ *   ints (1,048,576 pixels, 4 MiB) per device.  npix above that limit returns
+ *   DPL_ERR_UNSUPPORTED.  The call zeroes the array's counter on `stream` itself;
+ *   nothing needs to start at zero.
+ * Set-up: the first call on a device (with that device current) resolves the array's
+ *   address (cudaGetSymbolAddress, which also loads the module's data if it is not yet
+ *   loaded); make that first call before any stream capture.
+ * Calls that overlap on one device (other streams or threads) share the array and
+ *   race: serialise them. */
+int64_t dpl_process_coherence_noalloc_max_pixels(void);
+dpl_status dpl_process_coherence_noalloc(const float* C, int64_t npix, int nslc, int use_evd,
+                                         double beta, double zero_correlation_threshold,
+                                         int reference_idx, double num_looks,
+                                         int first_real_slc_idx, int compute_crlb,
+                                         float* eig_vecs, float* eig_vals, uint8_t* estimator,
+                                         float* crlb_std_dev, float* temp_coh,
+                                         float* closure_phases, dpl_stream_t stream);
+
 /* Kernel timing (no reference counterpart: a measurement hook).  While enabled,
  * dpl_phase_link records CUDA event pairs on its stream around the covariance
  * kernel (slot 0) and the solver kernel (slot 1; the plain form fuses both into
