@@ -182,6 +182,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(values, dist, device=None):
+    """Element-wise maximum of per-rank timings (every rank gets the result)."""
+    import torch
+
+    vals = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist is not None and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    return vals.tolist()
+
+
 def gpu_step(stack, plan, dp, outputs):
     """One pass of the hot path over every block of a device-resident stack."""
     cpx_full, tc_full = outputs
@@ -284,11 +294,7 @@ def run_ours(args, rank, world, pool, cores):
     h2d = host_stack.numel() * host_stack.element_size()
     d2h = host_cpx.numel() * host_cpx.element_size() + host_tc.numel() * host_tc.element_size()
 
-    # max over ranks
-    vals = torch.tensor([ms, e2e_ms, cov_ms, sol_ms], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
-    ms, e2e_ms, cov_ms, sol_ms = vals.tolist()
+    ms, e2e_ms, cov_ms, sol_ms = max_over_ranks([ms, e2e_ms, cov_ms, sol_ms], dist, dev)
     if rank != 0:
         return
     px = frame * frame * world
@@ -314,7 +320,8 @@ def run_ours(args, rank, world, pool, cores):
         cv, cd = cpu_sample(pool, cores)
         cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": cd + " (numpy restatement of the reference algorithm)"}
-    launches_per_step = len(plan) * 7  # k_ps_block, k_glrt_scale, k_glrt, k_prep, k_cov_tc, k_pixel, k_post
+    # per block: k_ps_block, k_glrt_scale, k_glrt, k_prep, k_cov_tc, k_pixel (solve), k_pixel (LU list), k_post
+    launches_per_step = len(plan) * 8
     line = {
         "metric": METRIC,
         "value": value,
