@@ -1,0 +1,361 @@
+// Register-resident per-pixel solver for N <= K (K = 16 or 32): one warp per pixel,
+// lane i owns row i of each matrix in registers.
+//
+// Same algorithms, iteration rules and outputs as solve_pixel (solver.cuh), laid out
+// for the register file instead of shared memory:
+//   |Gamma| + 1e-6 I  -> symmetric sweep (Gauss-Jordan in the "sweep" form: after
+//        sweeping every index the matrix holds -A^{-1}).  A non-positive pivot is
+//        the reference's Cholesky failure (_core.py:466-472, 496-515): EVD fallback.
+//   CRLB: the Fisher matrix (crlb.py:132-189) is swept the same way.
+//   EMI: A - 0.99 I (A = |Gamma|^{-1} o C) is inverted by the Hermitian sweep, and
+//        inverse iteration (_eigenvalues.py:139-205) is a matrix-vector product per
+//        step.  The sweep's pivots are those of the Cholesky/LDL^H factorisation, so
+//        a non-positive pivot is exactly "not positive definite": such a pixel is
+//        listed for the LU pass (the reference's LU algorithm), as in solve_pixel.
+//   EVD: power iteration on C o |C| with the rows in registers (_eigenvalues.py:93-136).
+//
+// Register rotation keeps the sweeps in compact loops: before step k, slot s of a
+// row holds column (k + s) mod K, so the pivot column is always slot 0 and each
+// update writes slot s - 1 from slot s (the shift costs nothing).  The column is
+// broadcast through shared memory at position (row - k) mod K, so slot s reads
+// position s.  Rows and columns >= N are zero and stay zero.
+#pragma once
+
+namespace dpl {
+
+// Shared memory per warp: full Hermitian C (n x ld, ld odd: a lane-per-row access of
+// one column is conflict-free), |Gamma|^{-1} (n x ld floats), a 32-entry broadcast
+// buffer and a 32-entry vector buffer.
+struct RegLayout {
+    int ld;
+    size_t off_C, off_G, off_b, off_w, bytes;
+};
+
+inline RegLayout make_reg_layout(int n) {
+    RegLayout L{};
+    L.ld = n | 1;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = align_up(o + bytes, 16);
+        return at;
+    };
+    L.off_C = take((size_t)n * L.ld * sizeof(cfloat));
+    L.off_G = take((size_t)n * L.ld * sizeof(float));
+    L.off_b = take(32 * sizeof(cfloat));
+    L.off_w = take(32 * sizeof(cfloat));
+    L.bytes = align_up(o, 128);
+    return L;
+}
+
+// Real symmetric sweep over indices 0..n-1 of the matrix whose row `lane` is g; on
+// success g holds row `lane` of -A^{-1}.  Returns false (uniformly) on a pivot <= 0.
+template <int K>
+__device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int lane) {
+#pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        __syncwarp();
+        if (lane < K) buf[(lane - k) & (K - 1)] = g[0];  // A[lane][k] (= A[k][lane])
+        __syncwarp();
+        float r[K];
+        const float4* b4 = reinterpret_cast<const float4*>(buf);
+#pragma unroll
+        for (int q = 0; q < K / 4; ++q) {
+            const float4 t = b4[q];
+            r[4 * q] = t.x;
+            r[4 * q + 1] = t.y;
+            r[4 * q + 2] = t.z;
+            r[4 * q + 3] = t.w;
+        }
+        const float p = r[0];
+        if (!(p > 0.f)) return false;
+        const float ip = 1.f / p;
+        const bool me = lane == k;
+        // rows i != k: a_ij - (a_ik / p) a_kj; row k: a_kj / p, written as
+        // a_kj - (1 - 1/p) a_kj so that every lane runs the same FMA
+        const float t = me ? 1.f - ip : g[0] * ip;
+        const float last = me ? -ip : g[0] * ip;
+#pragma unroll
+        for (int s = 0; s < K - 1; ++s) g[s] = fmaf(-t, r[s + 1], g[s + 1]);
+        g[K - 1] = last;
+    }
+#pragma unroll 1
+    for (int k = n; k < K; ++k) {  // finish the rotation: slot s holds column s again
+        const float t0 = g[0];
+#pragma unroll
+        for (int s = 0; s < K - 1; ++s) g[s] = g[s + 1];
+        g[K - 1] = t0;
+    }
+    __syncwarp();
+    return true;
+}
+
+// Hermitian sweep: on success a holds row `lane` of -A^{-1}.  False on a pivot <= 0.
+template <int K>
+__device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, int lane) {
+#pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        __syncwarp();
+        if (lane < K) buf[(lane - k) & (K - 1)] = a[0];  // A[lane][k] = conj(A[k][lane])
+        __syncwarp();
+        const float p = buf[0].re;
+        if (!(p > 0.f)) return false;
+        const float ip = 1.f / p;
+        const bool me = lane == k;
+        const cfloat t = me ? cmake(1.f - ip, 0.f) : cscale(a[0], ip);
+        const cfloat last = me ? cmake(-ip, 0.f) : cscale(a[0], ip);
+        const float4* b4 = reinterpret_cast<const float4*>(buf);
+#pragma unroll
+        for (int q = 0; q < K / 2; ++q) {
+            const float4 b = b4[q];
+            // slot s: a_ij - t a_kj, a_kj = conj(buffer entry s)
+            if (q > 0) a[2 * q - 1] = csub(a[2 * q], cmulc(t, cmake(b.x, b.y)));
+            a[2 * q] = csub(a[2 * q + 1], cmulc(t, cmake(b.z, b.w)));
+        }
+        a[K - 1] = last;
+    }
+#pragma unroll 1
+    for (int k = n; k < K; ++k) {
+        const cfloat t0 = a[0];
+#pragma unroll
+        for (int s = 0; s < K - 1; ++s) a[s] = a[s + 1];
+        a[K - 1] = t0;
+    }
+    __syncwarp();
+    return true;
+}
+
+// y_lane = sum_j h[j] x_j (row `lane` of a matrix in registers); x published in vb
+template <int K>
+__device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloat* vb, int lane) {
+    __syncwarp();
+    vb[lane] = x;
+    __syncwarp();
+    const float4* v4 = reinterpret_cast<const float4*>(vb);
+    cfloat acc = cmake(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < K / 2; ++q) {
+        const float4 t = v4[q];
+        acc = cadd(acc, cmul(h[2 * q], cmake(t.x, t.y)));
+        acc = cadd(acc, cmul(h[2 * q + 1], cmake(t.z, t.w)));
+    }
+    return acc;
+}
+
+// Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps
+// (the reference's while-loop: iteration count starts at 1, stops below 50).
+template <class Op>
+__device__ __forceinline__ cfloat r_iterate(cfloat v, Op&& op) {
+    float diff = 1.f;
+    for (int it = 1; diff > 1e-5f && it < 50; ++it) {
+        cfloat x = op(v);
+        const float inv = 1.f / sqrtf(warp_sum(cabs2(x)));
+        x = cscale(x, inv);
+        diff = sqrtf(warp_sum(cabs2(csub(x, v))));
+        v = x;
+    }
+    return v;
+}
+
+// Full solve for one pixel whose Hermitian coherence matrix is in Cf (n x ld, both
+// triangles).  A pixel whose shifted EMI matrix is not positive definite is appended
+// to a.fb_list and left for the LU pass.
+template <int K>
+__device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, float* Gs, int ld, cfloat* cb,
+                                cfloat* wb, int lane) {
+    const int n = a.n;
+    const bool row = lane < n;
+    const cfloat* Ci = Cf + (row ? lane : 0) * ld;
+    if (a.closure && lane < n - 2) {
+        const cfloat c = cmulc(cmul(Cf[lane * ld + lane + 1], Cf[(lane + 1) * ld + lane + 2]), Cf[lane * ld + lane + 2]);
+        a.closure[p * (n - 2) + lane] = atan2f(c.im, c.re);
+    }
+    // |Gamma| + 1e-6 I -> -|Gamma|^{-1}
+    float g[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        float x = 0.f;
+        if (row && j < n) {
+            x = s_gamma(a, Ci[j], j == lane);
+            if (j == lane) x = fadd(x, 1e-6f);
+        }
+        g[j] = x;
+    }
+    bool inv_nan = !r_sweep<K>(g, n, reinterpret_cast<float*>(cb), lane);
+    if (!inv_nan) {
+        bool bad = false;
+#pragma unroll
+        for (int j = 0; j < K; ++j) bad |= isnan(g[j]);
+        inv_nan = warp_any(bad);
+    }
+    const bool evd = a.use_evd || inv_nan;
+
+    // CRLB: FIM = 2L (Gamma o Gamma^{-1} - I), row/col `ref` -> identity, + 1e-6 I
+    if (a.compute_crlb) {
+        const int ref = a.crlb_ref;
+        bool ok = false;
+        float dg = 0.f;
+        if (!inv_nan) {
+            float f[K];
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                float x = 0.f;
+                if (row && j < n) {
+                    if (lane == ref || j == ref) {
+                        x = j == lane ? 1.f : 0.f;
+                    } else {
+                        x = fmul(a.crlb_factor, fsub(fmul(s_gamma(a, Ci[j], j == lane), -g[j]), j == lane ? 1.f : 0.f));
+                        if (j == lane) x = fadd(x, 1e-6f);
+                    }
+                }
+                f[j] = x;
+            }
+            ok = r_sweep<K>(f, n, reinterpret_cast<float*>(cb), lane);
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if (j == lane) dg = f[j];
+        }
+        if (row) a.crlb[p * n + lane] = lane == ref ? 0.f : (ok ? sqrtf(-dg) : nanf(""));
+    } else if (row) {
+        a.crlb[p * n + lane] = 0.f;
+    }
+
+    cfloat v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
+    float lambda;
+    if (!evd) {
+        // keep |Gamma|^{-1} for lambda = v^H A v
+        if (row) {
+            float* Gi = Gs + lane * ld;
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if (j < n) Gi[j] = -g[j];
+        }
+        cfloat am[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            cfloat x = cmake(0.f, 0.f);
+            if (row && j < n) {
+                x = cscale(Ci[j], -g[j]);
+                if (j == lane) x.re = fsub(x.re, 0.99f);
+            }
+            am[j] = x;
+        }
+        if (!r_sweep_c<K>(am, n, cb, lane)) {
+            if (lane == 0) a.fb_list[atomicAdd(a.fb_count, 1)] = (int)p;
+            __syncwarp();
+            return;
+        }
+        // am = -(A - 0.99 I)^{-1}: x <- (A - 0.99 I)^{-1} v = -(am v)
+        v = r_iterate(v, [&](cfloat x) {
+            const cfloat y = r_matvec<K>(am, x, wb, lane);
+            return cmake(-y.re, -y.im);
+        });
+        // lambda = Re v^H A v, A_ij = |Gamma|^{-1}_ij C_ij
+        __syncwarp();
+        wb[lane] = v;
+        __syncwarp();
+        cfloat acc = cmake(0.f, 0.f);
+        if (row) {
+            const float* Gi = Gs + lane * ld;
+            for (int j = 0; j < n; ++j) acc = cadd(acc, cmul(cscale(Ci[j], Gi[j]), wb[j]));
+        }
+        const float n2 = warp_sum(cabs2(v));
+        lambda = warp_sum(v.re * acc.re + v.im * acc.im);
+        v = cscale(v, sqrtf((float)n) / sqrtf(n2));
+    } else {
+        cfloat h[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            cfloat x = cmake(0.f, 0.f);
+            if (row && j < n) {
+                const cfloat c = Ci[j];
+                x = cscale(c, sqrtf(c.re * c.re + c.im * c.im));
+            }
+            h[j] = x;
+        }
+        v = r_iterate(v, [&](cfloat x) { return r_matvec<K>(h, x, wb, lane); });
+        const cfloat y = r_matvec<K>(h, v, wb, lane);
+        lambda = warp_sum(v.re * y.re + v.im * y.im);
+    }
+    // reference to reference_idx
+    const cfloat rot = cconj(fphasor(shfl_c(v, a.ref_idx)));
+    v = cmul(v, rot);
+    if (row) a.vout[p * n + lane] = v;
+    if (lane == 0) {
+        a.eig[p] = lambda;
+        a.est[p] = evd ? 0 : 1;
+    }
+    // temporal coherence over pairs c < r: conj(phasor(C_rc) w_c conj(w_r))
+    __syncwarp();
+    wb[lane] = fphasor(v);
+    __syncwarp();
+    float sre = 0.f, sim = 0.f;
+    int cnt = 0;
+    for (int r = 1; r < n; ++r) {
+        const cfloat wr = wb[r];
+        if (lane < r) {
+            const cfloat u = fphasor(Cf[r * ld + lane]);
+            const cfloat t = cconj(cmulc(cmul(u, wb[lane]), wr));
+            if (!cisnan(t)) {
+                sre += t.re;
+                sim += t.im;
+                ++cnt;
+            }
+        }
+    }
+    sre = warp_sum(sre);
+    sim = warp_sum(sim);
+    cnt = warp_sum_int(cnt);
+    if (lane == 0) {
+        const float fc = (float)cnt;
+        const float tc = hypotf(sre / fc, sim / fc);
+        a.tcoh[p] = isfinite(tc) ? tc : 0.f;
+    }
+    __syncwarp();
+}
+
+// Solve-only pass over all pixels with the register solver (n <= K).  The coherence
+// comes planar (diag Re | lower Re | lower Im, pair (i, j), i > j, at i(i-1)/2 + j)
+// or as full (npix, n, n) matrices of which the lower triangle is read.
+template <int K>
+__global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
+    extern __shared__ __align__(16) unsigned char reg_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    unsigned char* base = reg_smem + warp * L.bytes;
+    cfloat* Cf = reinterpret_cast<cfloat*>(base + L.off_C);
+    float* Gs = reinterpret_cast<float*>(base + L.off_G);
+    cfloat* cb = reinterpret_cast<cfloat*>(base + L.off_b);
+    cfloat* wb = reinterpret_cast<cfloat*>(base + L.off_w);
+    const int n = a.n, ld = L.ld, lag = a.baseline_lag;
+    for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
+        __syncwarp();
+        if (a.Cplanar) {
+            const float* src = a.Cplanar + p * n * n;
+            const int O = n * (n - 1) / 2;
+            if (lane < n) Cf[lane * ld + lane] = cmake(src[lane], 0.f);
+            for (int i = 1; i < n; ++i) {
+                const int o = i * (i - 1) / 2;
+                if (lane < i) {
+                    cfloat c = cmake(src[n + o + lane], src[n + O + o + lane]);
+                    if (lag > 0 && i - lane >= lag) c = cmake(0.f, 0.f);
+                    Cf[i * ld + lane] = c;
+                    Cf[lane * ld + i] = cconj(c);
+                }
+            }
+        } else {
+            const cfloat* src = a.Cin + p * n * n;
+            for (int i = 0; i < n; ++i) {
+                if (lane <= i) {
+                    cfloat c = src[i * n + lane];
+                    if (lag > 0 && i - lane >= lag) c = cmake(0.f, 0.f);
+                    Cf[i * ld + lane] = c;
+                    if (lane < i) Cf[lane * ld + i] = cconj(c);
+                }
+            }
+        }
+        __syncwarp();
+        solve_pixel_reg<K>(a, p, Cf, Gs, ld, cb, wb, lane);
+    }
+}
+
+}  // namespace dpl
