@@ -72,6 +72,13 @@ __device__ __forceinline__ cfloat cmul(cfloat a, cfloat b) {
 __device__ __forceinline__ cfloat cmulc(cfloat a, cfloat b) {
     return {a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im};
 }
+// acc + x * y and acc - x * conj(y) as four fused multiply-adds
+__device__ __forceinline__ cfloat cfma(cfloat acc, cfloat x, cfloat y) {
+    return {fmaf(x.re, y.re, fmaf(-x.im, y.im, acc.re)), fmaf(x.re, y.im, fmaf(x.im, y.re, acc.im))};
+}
+__device__ __forceinline__ cfloat cfms_conj(cfloat acc, cfloat x, cfloat y) {
+    return {fmaf(-x.re, y.re, fmaf(-x.im, y.im, acc.re)), fmaf(-x.im, y.re, fmaf(x.re, y.im, acc.im))};
+}
 __device__ __forceinline__ cfloat cconj(cfloat a) { return {a.re, -a.im}; }
 __device__ __forceinline__ cfloat cscale(cfloat a, float s) { return {a.re * s, a.im * s}; }
 __device__ __forceinline__ float cabs2(cfloat a) { return a.re * a.re + a.im * a.im; }

@@ -69,7 +69,7 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int la
         }
         const float p = r[0];
         if (!(p > 0.f)) return false;
-        const float ip = 1.f / p;
+        const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
         const bool me = lane == k;
         // rows i != k: a_ij - (a_ik / p) a_kj; row k: a_kj / p, written as
         // a_kj - (1 - 1/p) a_kj so that every lane runs the same FMA
@@ -100,7 +100,7 @@ __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, in
         __syncwarp();
         const float p = buf[0].re;
         if (!(p > 0.f)) return false;
-        const float ip = 1.f / p;
+        const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
         const bool me = lane == k;
         const cfloat t = me ? cmake(1.f - ip, 0.f) : cscale(a[0], ip);
         const cfloat last = me ? cmake(-ip, 0.f) : cscale(a[0], ip);
@@ -109,8 +109,8 @@ __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, in
         for (int q = 0; q < K / 2; ++q) {
             const float4 b = b4[q];
             // slot s: a_ij - t a_kj, a_kj = conj(buffer entry s)
-            if (q > 0) a[2 * q - 1] = csub(a[2 * q], cmulc(t, cmake(b.x, b.y)));
-            a[2 * q] = csub(a[2 * q + 1], cmulc(t, cmake(b.z, b.w)));
+            if (q > 0) a[2 * q - 1] = cfms_conj(a[2 * q], t, cmake(b.x, b.y));
+            a[2 * q] = cfms_conj(a[2 * q + 1], t, cmake(b.z, b.w));
         }
         a[K - 1] = last;
     }
@@ -132,14 +132,14 @@ __device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloa
     vb[lane] = x;
     __syncwarp();
     const float4* v4 = reinterpret_cast<const float4*>(vb);
-    cfloat acc = cmake(0.f, 0.f);
+    cfloat acc0 = cmake(0.f, 0.f), acc1 = cmake(0.f, 0.f);
 #pragma unroll
     for (int q = 0; q < K / 2; ++q) {
         const float4 t = v4[q];
-        acc = cadd(acc, cmul(h[2 * q], cmake(t.x, t.y)));
-        acc = cadd(acc, cmul(h[2 * q + 1], cmake(t.z, t.w)));
+        acc0 = cfma(acc0, h[2 * q], cmake(t.x, t.y));
+        acc1 = cfma(acc1, h[2 * q + 1], cmake(t.z, t.w));
     }
-    return acc;
+    return cadd(acc0, acc1);
 }
 
 // Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps
@@ -170,13 +170,15 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         const cfloat c = cmulc(cmul(Cf[lane * ld + lane + 1], Cf[(lane + 1) * ld + lane + 2]), Cf[lane * ld + lane + 2]);
         a.closure[p * (n - 2) + lane] = atan2f(c.im, c.re);
     }
-    // |Gamma| + 1e-6 I -> -|Gamma|^{-1}
+    // |Gamma| + 1e-6 I -> -|Gamma|^{-1}; |Gamma| itself stays in Gs for the CRLB
     float g[K];
+    float* Gi = Gs + (row ? lane : 0) * ld;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         float x = 0.f;
         if (row && j < n) {
             x = s_gamma(a, Ci[j], j == lane);
+            Gi[j] = x;
             if (j == lane) x = fadd(x, 1e-6f);
         }
         g[j] = x;
@@ -204,7 +206,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
                     if (lane == ref || j == ref) {
                         x = j == lane ? 1.f : 0.f;
                     } else {
-                        x = fmul(a.crlb_factor, fsub(fmul(s_gamma(a, Ci[j], j == lane), -g[j]), j == lane ? 1.f : 0.f));
+                        x = fmul(a.crlb_factor, fsub(fmul(Gi[j], -g[j]), j == lane ? 1.f : 0.f));
                         if (j == lane) x = fadd(x, 1e-6f);
                     }
                 }
@@ -225,7 +227,6 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     if (!evd) {
         // keep |Gamma|^{-1} for lambda = v^H A v
         if (row) {
-            float* Gi = Gs + lane * ld;
 #pragma unroll
             for (int j = 0; j < K; ++j)
                 if (j < n) Gi[j] = -g[j];
@@ -256,8 +257,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         __syncwarp();
         cfloat acc = cmake(0.f, 0.f);
         if (row) {
-            const float* Gi = Gs + lane * ld;
-            for (int j = 0; j < n; ++j) acc = cadd(acc, cmul(cscale(Ci[j], Gi[j]), wb[j]));
+            for (int j = 0; j < n; ++j) acc = cfma(acc, cscale(Ci[j], Gi[j]), wb[j]);
         }
         const float n2 = warp_sum(cabs2(v));
         lambda = warp_sum(v.re * acc.re + v.im * acc.im);
