@@ -6,24 +6,29 @@
 //
 //   A[p][s]  0/1: sample s of the tile's input region lies in pixel p's (clamped)
 //            window and is an SHP of p (exact in bf16)
-//   B[e][s]  the real output e of the per-sample outer product z(s) z(s)^H:
-//            e <  N          Re z_i conj(z_i) = |z_i|^2            (diagonal)
-//            e <  N + O      Re z_i conj(z_j)  for i > j            (O = N(N-1)/2)
-//            e <  N + 2O     Im z_i conj(z_j)  for i > j
+//   B[e][s]  the real outputs of the per-sample outer product z(s) z(s)^H:
+//            e <  N                  |z_i|^2                     (diagonal)
+//            e =  N + 2o, N + 2o + 1 Re, Im of z_i conj(z_j) for the lower pair
+//                                    o = i(i-1)/2 + j, i > j
 //
 // B is split into bf16 hi + lo parts (x = hi + lo + O(2^-17 x)); both products
 // accumulate into one fp32 accumulator in tensor memory.  The N^2 real outputs are
-// computed in passes of at most 512 TMEM columns (2 passes for N <= 31); the
-// diagonal is in the first pass, so every pass can be normalised on the fly
-// (covariance.py:131-142: C = numer / sqrt(amp_i amp_j) where that is > 1e-6).
+// computed in passes of at most 512 TMEM columns, split at pair boundaries; the
+// diagonal is in the first pass, so every pass is normalised on the fly
+// (covariance.py:131-142: C = numer / sqrt(amp_i amp_j) where that is > 1e-6,
+// evaluated as numer * r_i * r_j with r = 1 / sqrt(amp), valid where r_i r_j < 1e6).
 //
-// Shared-memory operands use the canonical K-major, no-swizzle layout: 8-row x
-// 16-byte core matrices, LBO = 128 B between core matrices along K, SBO = 512 B
-// (KC = 32) between 8-row groups.  Two stages are double buffered: the CTA builds
-// chunk k+1 while the MMAs of chunk k run; one thread issues the MMAs and commits
-// them to the stage's mbarrier.  Every wait is bounded.
+// Pipeline per K chunk of 32 samples (16 warps, one CTA per SM, persistent):
+//   the chunk's samples were prefetched into shared memory by cp.async while the
+//   previous chunk was built; all warps build A (mask bits -> bf16) and B (products,
+//   hi/lo split with paired conversions) into one of two stages in the canonical
+//   K-major no-swizzle layout (8-row x 16-byte core matrices, LBO 128 B, SBO 512 B);
+//   one thread issues the MMAs and commits them to the stage's mbarrier, and the
+//   next build overlaps them.  Every wait is bounded.
+// Epilogue: each warp reads 32 pixels x 32 columns from TMEM (tcgen05.ld), transposes
+// through its own shared buffer and writes 128-byte rows of the planar output.
 //
-// Output: planar per pixel, Cg[p][0 .. N^2) in the column order above.
+// Output: planar per pixel, Cg[p][0 .. N^2): diagonal, then (Re, Im) per lower pair.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -32,8 +37,12 @@ namespace dpl {
 
 constexpr int kTcM = 128;        // pixels per tile (MMA M)
 constexpr int kTcKC = 32;        // samples per K chunk
-constexpr int kTcThreads = 256;  // 8 warps
+constexpr int kTcThreads = 512;  // 16 warps
+constexpr int kTcWarps = kTcThreads / 32;
 constexpr int kTcMaxPW = 512;    // TMEM columns per pass
+constexpr int kTcMaxPass = 12;
+constexpr int kTcTileR = 8, kTcTileC = 16;  // output pixels per tile (rows x cols), kTcTileR * kTcTileC = kTcM
+constexpr int kTcTbufBytes = kTcWarps * 32 * 33 * 4;  // epilogue transpose buffers
 constexpr uint32_t kTcWaitLimit = 1u << 26;
 
 struct TcArgs {
@@ -41,17 +50,20 @@ struct TcArgs {
     int tile_r, tile_c, tiles_r, tiles_c;
     int region_r, region_c;  // max region extent of a tile
     int kpad;                // region samples padded to a multiple of kTcKC
-    int npass, pw;           // passes and columns per pass (multiple of 16)
-    const cfloat* zt;        // (rows, cols, n) masked, pixel-major
-    const uint32_t* bits;    // (out_rows, out_cols, wy, wpr) or null (rectangular window)
-    const uint8_t* nb_u8;    // alternative mask input (out_rows, out_cols, wy, wx)
+    int npass;
+    int pair0[kTcMaxPass + 1];  // pass p covers pairs [pair0[p], pair0[p+1]); pass 0 also the diagonal
+    int pcols[kTcMaxPass];      // TMEM columns of pass p (multiple of 16)
+    int ld_r;                   // row stride of the per-pixel r = 1/sqrt(amp) table (odd)
+    const cfloat* zt;           // (rows, cols, n) masked, pixel-major
+    const uint32_t* bits;       // (out_rows, out_cols, wy, wpr) or null (rectangular window)
+    const uint8_t* nb_u8;       // alternative mask input (out_rows, out_cols, wy, wx)
     int wpr;
-    float* Cg;               // (out_rows * out_cols, n * n) planar output
-    int32_t* counts;         // (out_rows * out_cols) or null
+    float* Cg;                  // (out_rows * out_cols, n * n) planar output
+    int32_t* counts;            // (out_rows * out_cols) or null
     int* status;
-    // shared-memory carve (bytes from the aligned base)
-    int off_stage0, off_stage1, stage_a_bytes, stage_b_bytes;
-    int off_z, off_amp, off_col, off_mask, off_win, off_bar, smem_bytes;
+    // shared-memory carve (bytes from the 1024-aligned base)
+    int off_stage, stage_bytes, stage_a_bytes, plane_bytes;
+    int off_z, z_bytes, off_r, off_pair, off_mask, off_win, off_bar, smem_bytes;
 };
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -97,10 +109,47 @@ __device__ __forceinline__ int tc_off(int row, int k) {
     return (row >> 3) * (kTcKC / 8 * 128) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
-__device__ __forceinline__ uint32_t bf16x2(float lo_elem, float hi_elem) {
-    const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(lo_elem));
-    const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(hi_elem));
-    return a | (b << 16);
+// bf16 hi/lo split of two values, packed (first value in the low half)
+__device__ __forceinline__ void tc_split2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+// 8-byte asynchronous global -> shared copy; src_bytes = 0 writes zeros
+__device__ __forceinline__ void tc_cp8(void* dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(tc_smem(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+
+// Prefetch the samples of chunk `ch` (region samples [32 ch, 32 ch + 32)) into zs.
+__device__ __forceinline__ void tc_prefetch(const TcArgs& a, cfloat* zs, int ch, int rr0, int cc0, int tid) {
+    const int n = a.n;
+    const int k0 = ch * kTcKC;
+    for (int e = tid; e < kTcKC * n; e += kTcThreads) {
+        const int k = e / n, t = e - k * n;
+        const int sidx = k0 + k;
+        const int ry = sidx / a.region_c, cx = sidx - ry * a.region_c;
+        const int r = rr0 + ry, c = cc0 + cx;
+        const bool in = ry < a.region_r && r < a.rows && c < a.cols;
+        const cfloat* src = in ? a.zt + ((int64_t)r * a.cols + c) * n + t : a.zt;
+        tc_cp8(zs + e, src, in ? 8 : 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_ld32(uint32_t addr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
@@ -111,38 +160,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     const int O = n * (n - 1) / 2;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [0], [1]: stage MMA done
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + a.off_bar + 64);
-    cfloat* zs = reinterpret_cast<cfloat*>(sm + a.off_z);          // [kTcKC][n]
-    float* amp = reinterpret_cast<float*>(sm + a.off_amp);          // [128][n+1]
-    uint32_t* colmap = reinterpret_cast<uint32_t*>(sm + a.off_col); // [npass*pw]: i | j<<8 | kind<<16
+    cfloat* const zb0 = reinterpret_cast<cfloat*>(sm + a.off_z);
+    cfloat* const zb1 = reinterpret_cast<cfloat*>(sm + a.off_z + a.z_bytes);
+    float* rtab = reinterpret_cast<float*>(sm + a.off_r);           // [128][ld_r]: 1/sqrt(amp_i)
+    uint32_t* pairs = reinterpret_cast<uint32_t*>(sm + a.off_pair); // [O]: i | j << 16
     uint32_t* mask = reinterpret_cast<uint32_t*>(sm + a.off_mask);  // [128][wy][2]
     int* win = reinterpret_cast<int*>(sm + a.off_win);              // [128][2]: window origin in region
 
-    // column map and barriers
-    for (int c = tid; c < a.npass * a.pw; c += blockDim.x) {
-        uint32_t v;
-        if (c < n) {
-            v = (uint32_t)c | ((uint32_t)c << 8) | (0u << 16);
-        } else if (c < n + 2 * O) {
-            const int o = (c - n) % (O > 0 ? O : 1);
-            int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j
-            while (i * (i - 1) / 2 > o) --i;
-            while ((i + 1) * i / 2 <= o) ++i;
-            const int j = o - i * (i - 1) / 2;
-            v = (uint32_t)i | ((uint32_t)j << 8) | ((c < n + O ? 1u : 2u) << 16);
-        } else {
-            v = 3u << 16;  // padding
-        }
-        colmap[c] = v;
+    for (int o = tid; o < O; o += kTcThreads) {
+        int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j, 0 <= j < i
+        while (i * (i - 1) / 2 > o) --i;
+        while ((i + 1) * i / 2 <= o) ++i;
+        pairs[o] = (uint32_t)i | ((uint32_t)(o - i * (i - 1) / 2) << 16);
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&bars[0])), "r"(1));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&bars[1])), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const int ncols_alloc = a.pw <= 256 ? 256 : 512;
+    constexpr int kAlloc = kTcMaxPW;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
-                     "r"(ncols_alloc));
+                     "r"(kAlloc));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -152,16 +191,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     uint32_t phase[2] = {0u, 0u};
     uint32_t uses[2] = {0u, 0u};  // commits issued per stage (to know what to wait for)
     bool failed = false;
+    const int nchunks = a.kpad / kTcKC;
 
     const int ntiles = a.tiles_r * a.tiles_c;
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-        const int tr0 = (tile / a.tiles_c) * a.tile_r, tc0 = (tile % a.tiles_c) * a.tile_c;
+        const int tr0 = (tile / a.tiles_c) * kTcTileR, tc0 = (tile % a.tiles_c) * kTcTileC;
         // region origin: clamped window start of the tile's first output pixel
         const int rr0 = min(max(a.sy / 2 + tr0 * a.sy - a.hy, 0), a.rows - wy);
         const int cc0 = min(max(a.sx / 2 + tc0 * a.sx - a.hx, 0), a.cols - wx);
         // per-pixel window origin (in region coordinates) and mask bits
         if (tid < kTcM) {
-            const int pr = tr0 + tid / a.tile_c, pc = tc0 + tid % a.tile_c;
+            const int pr = tr0 + tid / kTcTileC, pc = tc0 + tid % kTcTileC;
             const bool ok = pr < a.out_rows && pc < a.out_cols;
             int cnt = 0;
             if (ok) {
@@ -192,86 +232,98 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 win[2 * tid + 1] = -100000;
             }
         }
-        __syncthreads();
-        const int nchunks = a.kpad / kTcKC;
         for (int pass = 0; pass < a.npass && !failed; ++pass) {
+            const int pp0 = a.pair0[pass], npairs = a.pair0[pass + 1] - pp0;
+            const int ndiag = pass == 0 ? n : 0;
+            const int pcols = a.pcols[pass];
+            const int gbase = pass == 0 ? 0 : n + 2 * pp0;  // output column of TMEM column 0
+            const int gend = ndiag + 2 * npairs;            // TMEM columns holding outputs
+            tc_prefetch(a, zb0, 0, rr0, cc0, tid);
             for (int ch = 0; ch < nchunks; ++ch) {
                 const int s = ch & 1;
-                unsigned char* stage = sm + (s ? a.off_stage1 : a.off_stage0);
-                unsigned char* sA = stage;
-                unsigned char* sB = stage + a.stage_a_bytes;
+                unsigned char* sA = sm + a.off_stage + s * a.stage_bytes;
+                unsigned char* sBh = sA + a.stage_a_bytes;
+                unsigned char* sBl = sBh + a.plane_bytes;
                 // wait until the MMAs that last read this stage are done
                 if (uses[s] > 0) {
                     if (!tc_wait(&bars[s], phase[s])) failed = true;
                     phase[s] ^= 1u;
                     uses[s] = 0;
                 }
+                asm volatile("cp.async.wait_group 0;" ::: "memory");
                 if (__syncthreads_or(failed)) {
                     failed = true;
                     break;
                 }
-                // stage the chunk's samples: zs[k][t]
+                if (ch + 1 < nchunks) tc_prefetch(a, (ch & 1) ? zb0 : zb1, ch + 1, rr0, cc0, tid);
+                const cfloat* zs = (ch & 1) ? zb1 : zb0;
                 const int k0 = ch * kTcKC;
-                for (int e = tid; e < kTcKC * n; e += blockDim.x) {
-                    const int k = e / n, t = e - k * n;
-                    const int sidx = k0 + k;
-                    const int ry = sidx / a.region_c, cx = sidx - ry * a.region_c;
-                    const int r = rr0 + ry, c = cc0 + cx;
-                    cfloat z = cmake(0.f, 0.f);
-                    if (ry < a.region_r && r < a.rows && c < a.cols) z = a.zt[((int64_t)r * a.cols + c) * n + t];
-                    zs[k * n + t] = z;
-                }
-                __syncthreads();
-                // A: mask rows (thread -> pixel row, half of the chunk)
+                // A: thread -> (pixel row, 8 samples)
                 {
-                    const int row = tid >> 1, half = tid & 1;
+                    const int row = tid >> 2, g = tid & 3;
                     const int wr = win[2 * row], wc = win[2 * row + 1];
-                    for (int g = 0; g < 2; ++g) {
-                        const int kb = half * 16 + g * 8;
-                        uint32_t w4[4];
+                    const int s0 = k0 + 8 * g;
+                    int ry = s0 / a.region_c, cx = s0 - ry * a.region_c;
+                    uint32_t w4[4];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            float v2[2];
-#pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                const int sidx = k0 + kb + 2 * q + h;
-                                const int ry = sidx / a.region_c, cx = sidx - ry * a.region_c;
-                                const int dr = ry - wr, dc = cx - wc;
-                                float mv = 0.f;
-                                if (dr >= 0 && dr < wy && dc >= 0 && dc < wx && ry < a.region_r) {
-                                    const uint32_t wd = mask[(row * wy + dr) * 2 + (dc >> 5)];
-                                    mv = ((wd >> (dc & 31)) & 1u) ? 1.f : 0.f;
-                                }
-                                v2[h] = mv;
-                            }
-                            w4[q] = bf16x2(v2[0], v2[1]);
+                    for (int q = 0; q < 8; ++q) {
+                        const int dr = ry - wr, dc = cx - wc;
+                        uint32_t bit = 0u;
+                        if (dr >= 0 && dr < wy && dc >= 0 && dc < wx && ry < a.region_r)
+                            bit = (mask[(row * wy + dr) * 2 + (dc >> 5)] >> (dc & 31)) & 1u;
+                        const uint32_t hv = bit ? 0x3F80u : 0u;  // bf16 1.0 or 0
+                        if (q & 1) w4[q >> 1] |= hv << 16;
+                        else w4[q >> 1] = hv;
+                        if (++cx == a.region_c) {
+                            cx = 0;
+                            ++ry;
                         }
-                        *reinterpret_cast<uint4*>(sA + tc_off(row, kb)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
                     }
+                    *reinterpret_cast<uint4*>(sA + tc_off(row, 8 * g)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
                 }
-                // B: hi and lo planes, rows = this pass's output columns
-                for (int e = tid; e < a.pw; e += blockDim.x) {
-                    const uint32_t cm = colmap[pass * a.pw + e];
-                    const int i = cm & 0xff, j = (cm >> 8) & 0xff, kind = cm >> 16;
-                    for (int kb = 0; kb < kTcKC; kb += 8) {
-                        float hv[8], lv[8];
+                // B: tasks (diagonal i or pair o) x (8 samples), sample group outermost so
+                // that a warp reads one group of samples
+                {
+                    const int units = ndiag + npairs;
+                    for (int t = tid; t < 4 * units; t += kTcThreads) {
+                        const int g = t / units, u = t - g * units;
+                        const int kb = 8 * g;
+                        uint4 hw, lw;
+                        if (u < ndiag) {
+                            float x[8];
 #pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            float x = 0.f;
-                            if (kind < 3) {
+                            for (int q = 0; q < 8; ++q) x[q] = cabs2(zs[(kb + q) * n + u]);
+                            tc_split2(x[0], x[1], hw.x, lw.x);
+                            tc_split2(x[2], x[3], hw.y, lw.y);
+                            tc_split2(x[4], x[5], hw.z, lw.z);
+                            tc_split2(x[6], x[7], hw.w, lw.w);
+                            *reinterpret_cast<uint4*>(sBh + tc_off(u, kb)) = hw;
+                            *reinterpret_cast<uint4*>(sBl + tc_off(u, kb)) = lw;
+                        } else {
+                            const int o = u - ndiag;
+                            const uint32_t ij = pairs[pp0 + o];
+                            const int i = ij & 0xffff, j = ij >> 16;
+                            float re[8], im[8];
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
                                 const cfloat zi = zs[(kb + q) * n + i], zj = zs[(kb + q) * n + j];
-                                x = kind == 2 ? (zi.im * zj.re - zi.re * zj.im) : (zi.re * zj.re + zi.im * zj.im);
+                                re[q] = fmaf(zi.re, zj.re, zi.im * zj.im);    // Re z_i conj(z_j)
+                                im[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
                             }
-                            const __nv_bfloat16 hb = __float2bfloat16_rn(x);
-                            hv[q] = __bfloat162float(hb);
-                            lv[q] = x - hv[q];
+                            const int col = ndiag + 2 * o;
+                            tc_split2(re[0], re[1], hw.x, lw.x);
+                            tc_split2(re[2], re[3], hw.y, lw.y);
+                            tc_split2(re[4], re[5], hw.z, lw.z);
+                            tc_split2(re[6], re[7], hw.w, lw.w);
+                            *reinterpret_cast<uint4*>(sBh + tc_off(col, kb)) = hw;
+                            *reinterpret_cast<uint4*>(sBl + tc_off(col, kb)) = lw;
+                            tc_split2(im[0], im[1], hw.x, lw.x);
+                            tc_split2(im[2], im[3], hw.y, lw.y);
+                            tc_split2(im[4], im[5], hw.z, lw.z);
+                            tc_split2(im[6], im[7], hw.w, lw.w);
+                            *reinterpret_cast<uint4*>(sBh + tc_off(col + 1, kb)) = hw;
+                            *reinterpret_cast<uint4*>(sBl + tc_off(col + 1, kb)) = lw;
                         }
-                        uint4 hw = make_uint4(bf16x2(hv[0], hv[1]), bf16x2(hv[2], hv[3]), bf16x2(hv[4], hv[5]),
-                                              bf16x2(hv[6], hv[7]));
-                        uint4 lw = make_uint4(bf16x2(lv[0], lv[1]), bf16x2(lv[2], lv[3]), bf16x2(lv[4], lv[5]),
-                                              bf16x2(lv[6], lv[7]));
-                        *reinterpret_cast<uint4*>(sB + tc_off(e, kb)) = hw;
-                        *reinterpret_cast<uint4*>(sB + a.stage_b_bytes / 2 + tc_off(e, kb)) = lw;
                     }
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -279,12 +331,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 __syncthreads();
                 if (tid == 0) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t a_base = tc_smem(sA), b_hi = tc_smem(sB), b_lo = b_hi + a.stage_b_bytes / 2;
+                    const uint32_t a_base = tc_smem(sA), b_hi = tc_smem(sBh), b_lo = tc_smem(sBl);
                     constexpr uint32_t LBO = 128, SBO = kTcKC / 8 * 128;
                     for (int kk = 0; kk < kTcKC; kk += 16) {
                         const uint64_t ad = tc_desc(a_base + (kk / 8) * LBO, LBO, SBO);
-                        for (int n0 = 0; n0 < a.pw; n0 += 256) {
-                            const int nw = min(256, a.pw - n0);
+                        for (int n0 = 0; n0 < pcols; n0 += 256) {
+                            const int nw = min(256, pcols - n0);
                             const uint32_t idesc = tc_idesc_bf16(kTcM, nw);
                             const uint32_t boff = (uint32_t)(n0 / 8) * SBO + (kk / 8) * LBO;
                             const uint32_t dt = tmem + (uint32_t)n0;
@@ -321,67 +373,69 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 failed = true;
                 break;
             }
-            // epilogue: warps 0-3 own TMEM lanes 0-127 (one pixel each)
-            float* stagef = reinterpret_cast<float*>(sm + a.off_stage0);  // [128][33]
-            const int p_loc = tid & 127;
-            const int pr = tr0 + p_loc / a.tile_c, pc = tc0 + p_loc % a.tile_c;
-            const bool pix_ok = pr < a.out_rows && pc < a.out_cols;
-            for (int c0 = 0; c0 < a.pw; c0 += 32) {
-                if (warp < 4) {
-                    uint32_t r[32];
-                    const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-                          "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-                          "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                        : "r"(addr));
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (pass == 0 && c0 == 0) {
-                        // the diagonal (|z_i|^2 sums) is columns 0..n-1 of pass 0 (n <= 64 <= pw)
+            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (pixels) and every
+            // fourth group of 32 columns starting at group w / 4
+            const int quarter = warp & 3, part = warp >> 2;
+            const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+            float* tbuf = reinterpret_cast<float*>(sm + a.off_stage) + warp * (32 * 33);
+            if (pass == 0) {
+                // the diagonal (|z_i|^2 sums) is columns 0..n-1 of pass 0: r_i = 1 / sqrt(amp_i)
+                if (part == 0) {
+                    for (int c0 = 0; c0 < n; c0 += 32) {
+                        uint32_t r[32];
+                        tc_ld32(tmem + lane_base + (uint32_t)c0, r);
+                        float* rrow = rtab + (quarter * 32 + lane) * a.ld_r;
+#pragma unroll
                         for (int q = 0; q < 32; ++q)
-                            if (q < n) amp[p_loc * (n + 1) + q] = __uint_as_float(r[q]);
-                    }
-                    if (pass == 0 && c0 == 32 && n > 32) {
-                        for (int q = 0; q < 32; ++q)
-                            if (32 + q < n) amp[p_loc * (n + 1) + 32 + q] = __uint_as_float(r[q]);
-                    }
-                    for (int q = 0; q < 32; ++q) stagef[p_loc * 33 + q] = __uint_as_float(r[q]);
-                }
-                __syncthreads();
-                // normalise and store: each warp writes 16 pixel rows x 32 columns (coalesced)
-                for (int rr = warp; rr < kTcM; rr += 8) {
-                    const int pr2 = tr0 + rr / a.tile_c, pc2 = tc0 + rr % a.tile_c;
-                    const int c = c0 + lane;
-                    const int gc = pass * a.pw + c;
-                    if (pr2 < a.out_rows && pc2 < a.out_cols && c < a.pw && gc < nn) {
-                        const uint32_t cm = colmap[gc];
-                        const int i = cm & 0xff, j = (cm >> 8) & 0xff;
-                        const float ai = amp[rr * (n + 1) + i], aj = amp[rr * (n + 1) + j];
-                        const float sq = fsqrt(fmul(ai, aj));
-                        const float x = stagef[rr * 33 + lane];
-                        const int64_t p = (int64_t)pr2 * a.out_cols + pc2;
-                        a.Cg[p * nn + gc] = sq > 1e-6f ? fdiv(x, sq) : 0.f;
+                            if (c0 + q < n) rrow[c0 + q] = 1.f / sqrtf(__uint_as_float(r[q]));
                     }
                 }
                 __syncthreads();
             }
-            (void)pix_ok;
+            for (int c0 = 32 * part; c0 < gend; c0 += 32 * 4) {
+                uint32_t r[32];
+                tc_ld32(tmem + lane_base + (uint32_t)c0, r);
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < 32; ++q) tbuf[lane * 33 + q] = __uint_as_float(r[q]);
+                __syncwarp();
+                // lane -> column c0 + lane and its (i, j)
+                const int c = c0 + lane;
+                int ci = 0, cj = 0;
+                if (c < gend) {
+                    if (c < ndiag) {
+                        ci = cj = c;
+                    } else {
+                        const uint32_t ij = pairs[pp0 + ((c - ndiag) >> 1)];
+                        ci = ij & 0xffff;
+                        cj = ij >> 16;
+                    }
+                }
+                for (int rr = 0; rr < 32; ++rr) {
+                    const int pl = quarter * 32 + rr;
+                    const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
+                    if (pr < a.out_rows && pc < a.out_cols && c < gend) {
+                        const float* rrow = rtab + pl * a.ld_r;
+                        const float f = rrow[ci] * rrow[cj];
+                        const float x = tbuf[rr * 33 + lane];
+                        const int64_t p = (int64_t)pr * a.out_cols + pc;
+                        a.Cg[p * nn + gbase + c] = f < 1e6f ? x * f : 0.f;
+                    }
+                }
+            }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         }
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     if (failed && tid == 0) atomicExch(a.status, (int)DPL_ERR_TIMEOUT);
     // before releasing TMEM make sure no MMA is still in flight (bounded)
     for (int s2 = 0; s2 < 2; ++s2)
         if (uses[s2] > 0) tc_wait(&bars[s2], phase[s2]);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols_alloc));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kAlloc));
 }
 
 }  // namespace dpl

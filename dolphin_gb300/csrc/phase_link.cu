@@ -156,7 +156,7 @@ struct PixArgs {
     const uint32_t* nb_bits; // (out_rows, out_cols, wy, wpr) or null
     int wpr;
     const cfloat* Cin;       // solve-only input: (npix, n, n)
-    const float* Cplanar;    // solve-only input, planar per pixel: diag Re | off-diag Re | off-diag Im
+    const float* Cplanar;    // solve-only input, planar per pixel: diagonal | (Re, Im) per lower pair
     int use_evd, beta_on;
     float one_minus_beta, beta, zct;
     int ref_idx, compute_crlb, crlb_ref, baseline_lag;
@@ -289,11 +289,10 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
             __syncwarp();
             if (a.Cplanar) {
                 const float* src = a.Cplanar + p * n * n;
-                const int O = n * (n - 1) / 2;
                 for (int i = 0; i < n; ++i)
                     for (int j = lane; j <= i; j += 32) {
                         const int o = i * (i - 1) / 2 + j;  // pair (i, j), i > j
-                        m.C[pk(i, j)] = i == j ? cmake(src[i], 0.f) : cmake(src[n + o], src[n + O + o]);
+                        m.C[pk(i, j)] = i == j ? cmake(src[i], 0.f) : cmake(src[n + 2 * o], src[n + 2 * o + 1]);
                     }
             } else {
                 const cfloat* src = a.Cin + p * n * n;
@@ -331,11 +330,10 @@ __global__ void k_unpack_planar(const float* __restrict__ Cg, int n, int64_t npi
     const int64_t p = e / nn;
     const int r = (int)(e - p * nn), i = r / n, j = r - i * n;
     const float* src = Cg + p * nn;
-    const int O = n * (n - 1) / 2;
     cfloat v;
     if (i == j) v = cmake(src[i], 0.f);
-    else if (i > j) v = cmake(src[n + i * (i - 1) / 2 + j], src[n + O + i * (i - 1) / 2 + j]);
-    else v = cmake(src[n + j * (j - 1) / 2 + i], -src[n + O + j * (j - 1) / 2 + i]);
+    else if (i > j) v = cmake(src[n + 2 * (i * (i - 1) / 2 + j)], src[n + 2 * (i * (i - 1) / 2 + j) + 1]);
+    else v = cmake(src[n + 2 * (j * (j - 1) / 2 + i)], -src[n + 2 * (j * (j - 1) / 2 + i) + 1]);
     out[e] = v;
 }
 
@@ -539,10 +537,9 @@ static size_t tc_cov_bytes(int n, int64_t out_rows, int64_t out_cols) {
     return (size_t)out_rows * out_cols * n * n * sizeof(float);
 }
 
-static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int sy, int sx, const cfloat* zt,
-                                const uint32_t* bits, int wpr, const uint8_t* nb_u8, float* Cg, int32_t* counts,
-                                int* status, cudaStream_t s) {
-    TcArgs a{};
+// Tile, pass and shared-memory plan of the tensor-core covariance.  False if the
+// shape does not fit (then the plain SIMT form is used).
+static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, int sy, int sx) {
     a.n = n;
     a.rows = rows;
     a.cols = cols;
@@ -552,26 +549,38 @@ static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int s
     a.sx = sx;
     a.out_rows = rows / sy;
     a.out_cols = cols / sx;
-    if (a.out_rows == 0 || a.out_cols == 0) return DPL_OK;
     const int wy = 2 * hy + 1, wx = 2 * hx + 1;
-    a.tile_r = 8;
-    a.tile_c = 16;
-    a.tiles_r = ceil_div(a.out_rows, a.tile_r);
-    a.tiles_c = ceil_div(a.out_cols, a.tile_c);
+    if (wx > 64 || n < 1 || n > 64) return false;
+    a.tile_r = kTcTileR;
+    a.tile_c = kTcTileC;
+    a.tiles_r = ceil_div(std::max(a.out_rows, 1), a.tile_r);
+    a.tiles_c = ceil_div(std::max(a.out_cols, 1), a.tile_c);
     a.region_r = (a.tile_r - 1) * sy + wy;
     a.region_c = (a.tile_c - 1) * sx + wx;
-    a.kpad = ceil_div((int64_t)a.region_r * a.region_c, kTcKC) * kTcKC;
-    const int nn = n * n;
-    a.npass = ceil_div(nn, kTcMaxPW);
-    a.pw = ceil_div(ceil_div(nn, a.npass), 16) * 16;
-    if (a.pw > kTcMaxPW || a.pw < n) return fail(DPL_ERR_UNSUPPORTED, "tensor-core covariance: unsupported N");
-    a.zt = zt;
-    a.bits = bits;
-    a.wpr = wpr;
-    a.nb_u8 = nb_u8;
-    a.Cg = Cg;
-    a.counts = counts;
-    a.status = status;
+    a.kpad = (int)(ceil_div((int64_t)a.region_r * a.region_c, kTcKC) * kTcKC);
+    // passes of <= 512 TMEM columns split at pair boundaries, pass 0 with the diagonal
+    const int O = n * (n - 1) / 2;
+    bool ok = false;
+    for (a.npass = std::max(1, ceil_div(n * n, kTcMaxPW)); a.npass <= kTcMaxPass && !ok; ++a.npass) {
+        const int target = ceil_div(n * n, a.npass);
+        int o = 0;
+        ok = true;
+        a.pair0[0] = 0;
+        for (int p = 0; p < a.npass; ++p) {
+            const int base = p == 0 ? n : 0;
+            const int cnt = p == a.npass - 1 ? O - o : std::min(O - o, std::max(0, (target - base) / 2));
+            const int cols_p = std::max(16, ceil_div(base + 2 * cnt, 16) * 16);
+            if (cols_p > kTcMaxPW) ok = false;
+            a.pcols[p] = cols_p;
+            o += cnt;
+            a.pair0[p + 1] = o;
+        }
+        if (ok) break;
+    }
+    if (!ok) return false;
+    int pw_max = 0;
+    for (int p = 0; p < a.npass; ++p) pw_max = std::max(pw_max, a.pcols[p]);
+    a.ld_r = n | 1;
     size_t o = 0;
     auto take = [&](size_t bytes, size_t al) {
         o = align_up(o, al);
@@ -580,18 +589,33 @@ static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int s
         return (int)at;
     };
     a.stage_a_bytes = kTcM * kTcKC * 2;
-    a.stage_b_bytes = 2 * a.pw * kTcKC * 2;
-    const size_t stage = (size_t)a.stage_a_bytes + a.stage_b_bytes;
-    a.off_stage0 = take(std::max(stage, (size_t)kTcM * 33 * 4), 1024);
-    a.off_stage1 = take(stage, 1024);
-    a.off_z = take((size_t)kTcKC * n * sizeof(cfloat), 16);
-    a.off_amp = take((size_t)kTcM * (n + 1) * sizeof(float), 16);
-    a.off_col = take((size_t)a.npass * a.pw * sizeof(uint32_t), 16);
+    a.plane_bytes = pw_max * kTcKC * 2;
+    a.stage_bytes = (int)align_up((size_t)a.stage_a_bytes + 2 * (size_t)a.plane_bytes, 1024);
+    a.off_stage = take(std::max((size_t)2 * a.stage_bytes, (size_t)kTcTbufBytes), 1024);
+    a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
+    a.off_z = take(2 * (size_t)a.z_bytes, 16);
+    a.off_r = take((size_t)kTcM * a.ld_r * sizeof(float), 16);
+    a.off_pair = take((size_t)std::max(O, 1) * sizeof(uint32_t), 16);
     a.off_mask = take((size_t)kTcM * wy * 2 * sizeof(uint32_t), 16);
     a.off_win = take((size_t)kTcM * 2 * sizeof(int), 16);
     a.off_bar = take(128, 64);
     a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
-    if (a.smem_bytes > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "tensor-core covariance: window too large");
+    return a.smem_bytes <= 227 * 1024;
+}
+
+static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int sy, int sx, const cfloat* zt,
+                                const uint32_t* bits, int wpr, const uint8_t* nb_u8, float* Cg, int32_t* counts,
+                                int* status, cudaStream_t s) {
+    TcArgs a{};
+    if (!tc_configure(a, n, rows, cols, hy, hx, sy, sx)) return fail(DPL_ERR_UNSUPPORTED, "tensor-core covariance: unsupported shape");
+    if (a.out_rows == 0 || a.out_cols == 0) return DPL_OK;
+    a.zt = zt;
+    a.bits = bits;
+    a.wpr = wpr;
+    a.nb_u8 = nb_u8;
+    a.Cg = Cg;
+    a.counts = counts;
+    a.status = status;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -722,7 +746,9 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
         a.tcoh = out->temp_coh;
         a.closure = n > 2 ? out->closure_phases : nullptr;
         a.counts = in->neighbors ? out->shp_counts : nullptr;
-        if (P.cov_form == 0) {
+        TcArgs tcfit{};
+        const bool tc_fits = P.cov_form == 0 && tc_configure(tcfit, n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx);
+        if (tc_fits) {
             // chosen form: tensor-core covariance, then the solver on the planar matrices
             st = timed(s, 0, [&] {
                 return launch_cov_tc(n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, w.zt, nullptr, 0,
@@ -732,7 +758,8 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
             a.Cplanar = w.Cg;
             st = timed(s, 1, [&] { return launch_pixel<kSolveOnly>(a, s, w.fb); });
         } else {
-            // plain form: SIMT covariance fused with the solver
+            // plain form (or a window too large for the tensor-core tiles): SIMT covariance
+            // fused with the solver
             st = timed(s, 0, [&] { return launch_pixel<kFused>(a, s, w.fb); });
         }
         if (st != DPL_OK) return st;
@@ -830,7 +857,9 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
     a.zt = zt;
     a.nb_u8 = neighbors;
     a.Cout = reinterpret_cast<cfloat*>(C);
-    if (cov_form == 1) return launch_pixel<kCovOnly>(a, s);
+    TcArgs tcfit{};
+    if (cov_form == 1 || !tc_configure(tcfit, n, (int)rows, (int)cols, hy, hx, sy, sx))
+        return launch_pixel<kCovOnly>(a, s);
     DPL_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
     st = launch_cov_tc(n, (int)rows, (int)cols, hy, hx, sy, sx, zt, nullptr, 0, neighbors, Cg, nullptr, status, s);
     if (st != DPL_OK) return st;

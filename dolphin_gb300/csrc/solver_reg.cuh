@@ -315,7 +315,8 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
 }
 
 // Solve-only pass over all pixels with the register solver (n <= K).  The coherence
-// comes planar (diag Re | lower Re | lower Im, pair (i, j), i > j, at i(i-1)/2 + j)
+// comes planar (diagonal, then (Re, Im) of the lower pair (i, j), i > j, at
+// o = i(i-1)/2 + j)
 // or as full (npix, n, n) matrices of which the lower triangle is read.
 template <int K>
 __global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
@@ -331,12 +332,11 @@ __global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
         __syncwarp();
         if (a.Cplanar) {
             const float* src = a.Cplanar + p * n * n;
-            const int O = n * (n - 1) / 2;
             if (lane < n) Cf[lane * ld + lane] = cmake(src[lane], 0.f);
             for (int i = 1; i < n; ++i) {
                 const int o = i * (i - 1) / 2;
                 if (lane < i) {
-                    cfloat c = cmake(src[n + o + lane], src[n + O + o + lane]);
+                    cfloat c = cmake(src[n + 2 * (o + lane)], src[n + 2 * (o + lane) + 1]);
                     if (lag > 0 && i - lane >= lag) c = cmake(0.f, 0.f);
                     Cf[i * ld + lane] = c;
                     Cf[lane * ld + i] = cconj(c);
