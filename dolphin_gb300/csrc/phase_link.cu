@@ -496,7 +496,7 @@ static dpl_status launch_pixel_pass(const PixArgs& a, cudaStream_t s) {
 static dpl_status launch_solve_reg(const PixArgs& a, cudaStream_t s) {
     const RegLayout L = make_reg_layout(a.n);
     const int warps = 8;
-    const size_t smem = (size_t)warps * L.bytes;
+    const size_t smem = (size_t)warps * L.bytes + (size_t)a.n * (a.n - 1) / 2 * sizeof(uint32_t);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

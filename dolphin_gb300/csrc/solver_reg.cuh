@@ -49,9 +49,11 @@ inline RegLayout make_reg_layout(int n) {
 }
 
 // Real symmetric sweep over indices 0..n-1 of the matrix whose row `lane` is g; on
-// success g holds row `lane` of -A^{-1}.  Returns false (uniformly) on a pivot <= 0.
+// success g holds row `lane` of -A^{-1}.  Returns false (uniformly) if any pivot was
+// <= 0 (the remaining steps then run on meaningless values, without branching).
 template <int K>
 __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int lane) {
+    bool bad = false;  // uniform: every lane reads the same pivot
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
         __syncwarp();
@@ -68,7 +70,7 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int la
             r[4 * q + 3] = t.w;
         }
         const float p = r[0];
-        if (!(p > 0.f)) return false;
+        bad |= !(p > 0.f);
         const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
         const bool me = lane == k;
         // rows i != k: a_ij - (a_ik / p) a_kj; row k: a_kj / p, written as
@@ -87,19 +89,20 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int la
         g[K - 1] = t0;
     }
     __syncwarp();
-    return true;
+    return !bad;
 }
 
-// Hermitian sweep: on success a holds row `lane` of -A^{-1}.  False on a pivot <= 0.
+// Hermitian sweep: on success a holds row `lane` of -A^{-1}.  False if a pivot was <= 0.
 template <int K>
 __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, int lane) {
+    bool bad = false;  // uniform: every lane reads the same pivot
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
         __syncwarp();
         if (lane < K) buf[(lane - k) & (K - 1)] = a[0];  // A[lane][k] = conj(A[k][lane])
         __syncwarp();
         const float p = buf[0].re;
-        if (!(p > 0.f)) return false;
+        bad |= !(p > 0.f);
         const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
         const bool me = lane == k;
         const cfloat t = me ? cmake(1.f - ip, 0.f) : cscale(a[0], ip);
@@ -122,7 +125,7 @@ __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, in
         a[K - 1] = t0;
     }
     __syncwarp();
-    return true;
+    return !bad;
 }
 
 // y_lane = sum_j h[j] x_j (row `lane` of a matrix in registers); x published in vb
@@ -162,7 +165,7 @@ __device__ __forceinline__ cfloat r_iterate(cfloat v, Op&& op) {
 // to a.fb_list and left for the LU pass.
 template <int K>
 __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, float* Gs, int ld, cfloat* cb,
-                                cfloat* wb, int lane) {
+                                cfloat* wb, const uint32_t* ptab, int lane) {
     const int n = a.n;
     const bool row = lane < n;
     const cfloat* Ci = Cf + (row ? lane : 0) * ld;
@@ -170,73 +173,74 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         const cfloat c = cmulc(cmul(Cf[lane * ld + lane + 1], Cf[(lane + 1) * ld + lane + 2]), Cf[lane * ld + lane + 2]);
         a.closure[p * (n - 2) + lane] = atan2f(c.im, c.re);
     }
-    // |Gamma| + 1e-6 I -> -|Gamma|^{-1}; |Gamma| itself stays in Gs for the CRLB
-    float g[K];
+    // |Gamma| + 1e-6 I -> -|Gamma|^{-1} (round 0), then the CRLB's Fisher matrix
+    // FIM = 2L (Gamma o Gamma^{-1} - I), row/col `ref` -> identity, + 1e-6 I (round 1).
+    // Gs holds |Gamma| during round 0 and |Gamma|^{-1} afterwards.
     float* Gi = Gs + (row ? lane : 0) * ld;
+    const int ref = a.crlb_ref;
+    bool inv_nan = true;
+    bool crlb_ok = false;
+    float dg = 0.f;
+    if (!(a.use_evd && !a.compute_crlb)) {
+        float g[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) {
-        float x = 0.f;
-        if (row && j < n) {
-            x = s_gamma(a, Ci[j], j == lane);
-            Gi[j] = x;
-            if (j == lane) x = fadd(x, 1e-6f);
+        for (int j = 0; j < K; ++j) {
+            float x = 0.f;
+            if (row && j < n) {
+                x = s_gamma(a, Ci[j], j == lane);
+                Gi[j] = x;
+                if (j == lane) x = fadd(x, 1e-6f);
+            }
+            g[j] = x;
         }
-        g[j] = x;
-    }
-    bool inv_nan = !r_sweep<K>(g, n, reinterpret_cast<float*>(cb), lane);
-    if (!inv_nan) {
-        bool bad = false;
+#pragma unroll 1
+        for (int round = 0; round < 2; ++round) {
+            const bool ok = r_sweep<K>(g, n, reinterpret_cast<float*>(cb), lane);
+            if (round == 1) {
+                crlb_ok = ok;
 #pragma unroll
-        for (int j = 0; j < K; ++j) bad |= isnan(g[j]);
-        inv_nan = warp_any(bad);
-    }
-    const bool evd = a.use_evd || inv_nan;
-
-    // CRLB: FIM = 2L (Gamma o Gamma^{-1} - I), row/col `ref` -> identity, + 1e-6 I
-    if (a.compute_crlb) {
-        const int ref = a.crlb_ref;
-        bool ok = false;
-        float dg = 0.f;
-        if (!inv_nan) {
-            float f[K];
+                for (int j = 0; j < K; ++j)
+                    if (j == lane) dg = g[j];
+                break;
+            }
+            inv_nan = !ok;
+            if (ok) {
+                bool bad = false;
+#pragma unroll
+                for (int j = 0; j < K; ++j) bad |= isnan(g[j]);
+                inv_nan = warp_any(bad);
+            }
+            // keep |Gamma|^{-1} and build the FIM in place of it
 #pragma unroll
             for (int j = 0; j < K; ++j) {
+                const float ginv = -g[j];
                 float x = 0.f;
                 if (row && j < n) {
                     if (lane == ref || j == ref) {
                         x = j == lane ? 1.f : 0.f;
                     } else {
-                        x = fmul(a.crlb_factor, fsub(fmul(Gi[j], -g[j]), j == lane ? 1.f : 0.f));
+                        x = fmul(a.crlb_factor, fsub(fmul(Gi[j], ginv), j == lane ? 1.f : 0.f));
                         if (j == lane) x = fadd(x, 1e-6f);
                     }
+                    Gi[j] = ginv;
                 }
-                f[j] = x;
+                g[j] = x;
             }
-            ok = r_sweep<K>(f, n, reinterpret_cast<float*>(cb), lane);
-#pragma unroll
-            for (int j = 0; j < K; ++j)
-                if (j == lane) dg = f[j];
+            if (!a.compute_crlb || inv_nan) break;
         }
-        if (row) a.crlb[p * n + lane] = lane == ref ? 0.f : (ok ? sqrtf(-dg) : nanf(""));
-    } else if (row) {
-        a.crlb[p * n + lane] = 0.f;
     }
+    const bool evd = a.use_evd || inv_nan;
+    if (row) a.crlb[p * n + lane] = !a.compute_crlb || lane == ref ? 0.f : (crlb_ok ? sqrtf(-dg) : nanf(""));
 
     cfloat v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
     float lambda;
     if (!evd) {
-        // keep |Gamma|^{-1} for lambda = v^H A v
-        if (row) {
-#pragma unroll
-            for (int j = 0; j < K; ++j)
-                if (j < n) Gi[j] = -g[j];
-        }
         cfloat am[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
             cfloat x = cmake(0.f, 0.f);
             if (row && j < n) {
-                x = cscale(Ci[j], -g[j]);
+                x = cscale(Ci[j], Gi[j]);
                 if (j == lane) x.re = fsub(x.re, 0.99f);
             }
             am[j] = x;
@@ -285,22 +289,23 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         a.eig[p] = lambda;
         a.est[p] = evd ? 0 : 1;
     }
-    // temporal coherence over pairs c < r: conj(phasor(C_rc) w_c conj(w_r))
+    // temporal coherence over pairs c < r (ptab: the lower pairs r | c << 16, row by
+    // row): conj(phasor(C_rc) w_c conj(w_r))
     __syncwarp();
     wb[lane] = fphasor(v);
     __syncwarp();
     float sre = 0.f, sim = 0.f;
     int cnt = 0;
-    for (int r = 1; r < n; ++r) {
-        const cfloat wr = wb[r];
-        if (lane < r) {
-            const cfloat u = fphasor(Cf[r * ld + lane]);
-            const cfloat t = cconj(cmulc(cmul(u, wb[lane]), wr));
-            if (!cisnan(t)) {
-                sre += t.re;
-                sim += t.im;
-                ++cnt;
-            }
+    const int npairs = n * (n - 1) / 2;
+    for (int e = lane; e < npairs; e += 32) {
+        const uint32_t rc = ptab[e];
+        const int r = rc & 0xffff, c = rc >> 16;
+        const cfloat u = fphasor(Cf[r * ld + c]);
+        const cfloat t = cconj(cmulc(cmul(u, wb[c]), wb[r]));
+        if (!cisnan(t)) {
+            sre += t.re;
+            sim += t.im;
+            ++cnt;
         }
     }
     sre = warp_sum(sre);
@@ -327,7 +332,15 @@ __global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
     float* Gs = reinterpret_cast<float*>(base + L.off_G);
     cfloat* cb = reinterpret_cast<cfloat*>(base + L.off_b);
     cfloat* wb = reinterpret_cast<cfloat*>(base + L.off_w);
+    uint32_t* ptab = reinterpret_cast<uint32_t*>(reg_smem + nwarps * L.bytes);  // shared by the CTA
     const int n = a.n, ld = L.ld, lag = a.baseline_lag;
+    for (int o = threadIdx.x; o < n * (n - 1) / 2; o += blockDim.x) {
+        int r = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = r(r-1)/2 + c, 0 <= c < r
+        while (r * (r - 1) / 2 > o) --r;
+        while ((r + 1) * r / 2 <= o) ++r;
+        ptab[o] = (uint32_t)r | ((uint32_t)(o - r * (r - 1) / 2) << 16);
+    }
+    __syncthreads();
     for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
         __syncwarp();
         if (a.Cplanar) {
@@ -354,7 +367,7 @@ __global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
             }
         }
         __syncwarp();
-        solve_pixel_reg<K>(a, p, Cf, Gs, ld, cb, wb, lane);
+        solve_pixel_reg<K>(a, p, Cf, Gs, ld, cb, wb, ptab, lane);
     }
 }
 
