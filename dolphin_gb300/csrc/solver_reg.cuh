@@ -145,6 +145,16 @@ __device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloa
     return cadd(acc0, acc1);
 }
 
+// Asynchronous copy of one pixel's planar coherence (count floats) into shared memory.
+__device__ __forceinline__ void r_prefetch(float* dst, const float* src, int count, int lane) {
+    __syncwarp();
+    for (int e = lane; e < count; e += 32)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + e)),
+                     "l"(src + e)
+                     : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 // Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps
 // (the reference's while-loop: iteration count starts at 1, stops below 50).
 template <class Op>
@@ -162,10 +172,11 @@ __device__ __forceinline__ cfloat r_iterate(cfloat v, Op&& op) {
 
 // Full solve for one pixel whose Hermitian coherence matrix is in Cf (n x ld, both
 // triangles).  A pixel whose shifted EMI matrix is not positive definite is appended
-// to a.fb_list and left for the LU pass.
+// to a.fb_list and left for the LU pass.  Once Gs is no longer needed, the planar
+// coherence of the warp's next pixel (`next`, if any) is prefetched into it.
 template <int K>
 __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, float* Gs, int ld, cfloat* cb,
-                                cfloat* wb, const uint32_t* ptab, int lane) {
+                                cfloat* wb, const uint32_t* ptab, const float* next, int lane) {
     const int n = a.n;
     const bool row = lane < n;
     const cfloat* Ci = Cf + (row ? lane : 0) * ld;
@@ -247,6 +258,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         }
         if (!r_sweep_c<K>(am, n, cb, lane)) {
             if (lane == 0) a.fb_list[atomicAdd(a.fb_count, 1)] = (int)p;
+            if (next) r_prefetch(Gs, next, n * n, lane);
             __syncwarp();
             return;
         }
@@ -263,10 +275,12 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         if (row) {
             for (int j = 0; j < n; ++j) acc = cfma(acc, cscale(Ci[j], Gi[j]), wb[j]);
         }
+        if (next) r_prefetch(Gs, next, n * n, lane);
         const float n2 = warp_sum(cabs2(v));
         lambda = warp_sum(v.re * acc.re + v.im * acc.im);
         v = cscale(v, sqrtf((float)n) / sqrtf(n2));
     } else {
+        if (next) r_prefetch(Gs, next, n * n, lane);
         cfloat h[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
@@ -341,10 +355,14 @@ __global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
         ptab[o] = (uint32_t)r | ((uint32_t)(o - r * (r - 1) / 2) << 16);
     }
     __syncthreads();
-    for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
+    const int64_t stride = (int64_t)gridDim.x * nwarps;
+    bool staged = false;  // Gs holds this pixel's planar coherence (prefetched)
+    for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += stride) {
         __syncwarp();
         if (a.Cplanar) {
-            const float* src = a.Cplanar + p * n * n;
+            if (staged) asm volatile("cp.async.wait_group 0;" ::: "memory");
+            __syncwarp();
+            const float* src = staged ? Gs : a.Cplanar + p * n * n;
             if (lane < n) Cf[lane * ld + lane] = cmake(src[lane], 0.f);
             for (int i = 1; i < n; ++i) {
                 const int o = i * (i - 1) / 2;
@@ -367,8 +385,11 @@ __global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
             }
         }
         __syncwarp();
-        solve_pixel_reg<K>(a, p, Cf, Gs, ld, cb, wb, ptab, lane);
+        const float* next = a.Cplanar && p + stride < a.npix ? a.Cplanar + (p + stride) * n * n : nullptr;
+        solve_pixel_reg<K>(a, p, Cf, Gs, ld, cb, wb, ptab, next, lane);
+        staged = next != nullptr;
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 }  // namespace dpl
