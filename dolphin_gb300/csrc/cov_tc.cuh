@@ -1,32 +1,34 @@
 // SHP-masked coherence matrices on the 5th-generation tensor cores (tcgen05).
 //
-// For a tile of 128 output pixels the sample covariance is one GEMM:
+// For a tile of 16 x 16 output pixels the sample covariance is one GEMM:
 //
-//     D[p][e] = sum_s  A[p][s] * B[e][s]
+//     D[e][p] = sum_s  KR[e][s] * M[p][s]
 //
-//   A[p][s]  0/1: sample s of the tile's input region lies in pixel p's (clamped)
-//            window and is an SHP of p (exact in bf16)
-//   B[e][s]  the real outputs of the per-sample outer product z(s) z(s)^H:
-//            e <  N                  |z_i|^2                     (diagonal)
-//            e =  N + 2o, N + 2o + 1 Re, Im of z_i conj(z_j) for the lower pair
-//                                    o = i(i-1)/2 + j, i > j
+//   KR[e][s]  the real components of the per-sample outer product z(s) z(s)^H
+//             (Khatri-Rao rows, the MMA's A operand, 128 rows per M tile):
+//             e <  N                  |z_i|^2                     (diagonal)
+//             e =  N + 2o, N + 2o + 1 Re, Im of z_i conj(z_j) for the lower pair
+//                                     o = i(i-1)/2 + j, i > j
+//   M[p][s]   0/1: sample s of the tile's input region lies in pixel p's (clamped)
+//             window and is an SHP of p (the B operand, N = 256 pixels; exact in bf16)
 //
-// B is split into bf16 hi + lo parts (x = hi + lo + O(2^-17 x)); both products
-// accumulate into one fp32 accumulator in tensor memory.  The N^2 real outputs are
-// computed in passes of at most 512 TMEM columns, split at pair boundaries; the
-// diagonal is in the first pass, so every pass is normalised on the fly
-// (covariance.py:131-142: C = numer / sqrt(amp_i amp_j) where that is > 1e-6,
-// evaluated as numer * r_i * r_j with r = 1 / sqrt(amp), valid where r_i r_j < 1e6).
+// KR is split into bf16 hi + lo parts (x = hi + lo + O(2^-17 x)); both products
+// accumulate into one fp32 accumulator in tensor memory.  A pass covers 256
+// components (two M tiles, 2 x 256 TMEM columns); the diagonal is in the first pass,
+// so every pass is normalised on the fly (covariance.py:131-142: C = numer /
+// sqrt(amp_i amp_j) where that is > 1e-6, evaluated as numer * r_i * r_j with
+// r = 1 / sqrt(amp), valid where r_i r_j < 1e6).
 //
-// Pipeline per K chunk of 32 samples (16 warps, one CTA per SM, persistent):
-//   the chunk's samples were prefetched into shared memory by cp.async while the
-//   previous chunk was built; all warps build A (mask bits -> bf16) and B (products,
-//   hi/lo split with paired conversions) into one of two stages in the canonical
-//   K-major no-swizzle layout (8-row x 16-byte core matrices, LBO 128 B, SBO 512 B);
-//   one thread issues the MMAs and commits them to the stage's mbarrier, and the
-//   next build overlaps them.  Every wait is bounded.
-// Epilogue: each warp reads 32 pixels x 32 columns from TMEM (tcgen05.ld), transposes
-// through its own shared buffer and writes 128-byte rows of the planar output.
+// Per tile the masks are turned once into per-pixel bit arrays over the region's
+// samples.  Per K chunk of 32 samples, warps 0-14 (builders) expand the chunk's mask
+// bits to bf16, form the KR rows of the pass from the chunk's samples (prefetched
+// into shared memory with cp.async while the previous chunk was built) and signal
+// the stage's `full` mbarrier; warp 15 waits on it, issues the MMAs (canonical
+// K-major no-swizzle layout: 8-row x 16-byte core matrices, LBO 128 B, SBO 512 B) and
+// commits them to the stage's `empty` mbarrier, which the builders wait on before
+// reusing the stage.  Every wait is bounded.
+// Epilogue: TMEM lane = component, column = pixel, so each tcgen05.ld row is one
+// component of 32 pixels and the planar output is written with coalesced stores.
 //
 // Output: planar per pixel, Cg[p][0 .. N^2): diagonal, then (Re, Im) per lower pair.
 #pragma once
@@ -35,35 +37,32 @@
 
 namespace dpl {
 
-constexpr int kTcM = 128;        // pixels per tile (MMA M)
-constexpr int kTcKC = 32;        // samples per K chunk
-constexpr int kTcThreads = 512;  // 16 warps
-constexpr int kTcWarps = kTcThreads / 32;
-constexpr int kTcMaxPW = 512;    // TMEM columns per pass
-constexpr int kTcMaxPass = 12;
-constexpr int kTcTileR = 8, kTcTileC = 16;  // output pixels per tile (rows x cols), kTcTileR * kTcTileC = kTcM
-constexpr int kTcTbufBytes = kTcWarps * 32 * 33 * 4;  // epilogue transpose buffers
+constexpr int kTcM = 128;                    // components per M tile
+constexpr int kTcN = 256;                    // pixels per tile (MMA N)
+constexpr int kTcTileR = 16, kTcTileC = 16;  // tile of output pixels
+constexpr int kTcKC = 32;                    // samples per K chunk
+constexpr int kTcThreads = 512;              // 16 warps
+constexpr int kTcBuilders = 480;             // warps 0-14; warp 15 issues the MMAs
+constexpr int kTcCols = 512;                 // TMEM columns: two M tiles x 256 pixels
+constexpr int kTcStageBytes = 4 * 8192 + 16384;  // KR hi/lo of two M tiles + mask
 constexpr uint32_t kTcWaitLimit = 1u << 26;
 
 struct TcArgs {
     int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
-    int tile_r, tile_c, tiles_r, tiles_c;
+    int tiles_r, tiles_c;
     int region_r, region_c;  // max region extent of a tile
-    int kpad;                // region samples padded to a multiple of kTcKC
-    int npass;
-    int pair0[kTcMaxPass + 1];  // pass p covers pairs [pair0[p], pair0[p+1]); pass 0 also the diagonal
-    int pcols[kTcMaxPass];      // TMEM columns of pass p (multiple of 16)
-    int ld_r;                   // row stride of the per-pixel r = 1/sqrt(amp) table (odd)
-    const cfloat* zt;           // (rows, cols, n) masked, pixel-major
-    const uint32_t* bits;       // (out_rows, out_cols, wy, wpr) or null (rectangular window)
-    const uint8_t* nb_u8;       // alternative mask input (out_rows, out_cols, wy, wx)
+    int kpad, kwords;        // region samples padded to a multiple of kTcKC; 32-bit words per pixel
+    int npass;               // ceil(N^2 / 256)
+    int ld_r;                // row stride of the per-pixel r = 1/sqrt(amp) table (odd)
+    const cfloat* zt;        // (rows, cols, n) masked, pixel-major
+    const uint32_t* bits;    // (out_rows, out_cols, wy, wpr) or null (rectangular window)
+    const uint8_t* nb_u8;    // alternative mask input (out_rows, out_cols, wy, wx)
     int wpr;
-    float* Cg;                  // (out_rows * out_cols, n * n) planar output
-    int32_t* counts;            // (out_rows * out_cols) or null
+    float* Cg;               // (out_rows * out_cols, n * n) planar output
+    int32_t* counts;         // (out_rows * out_cols) or null
     int* status;
     // shared-memory carve (bytes from the 1024-aligned base)
-    int off_stage, stage_bytes, stage_a_bytes, plane_bytes;
-    int off_z, z_bytes, off_r, off_pair, off_mask, off_win, off_bar, smem_bytes;
+    int off_stage, off_z, z_bytes, off_r, off_pbits, off_soff, off_pair, off_bar, smem_bytes;
 };
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -118,26 +117,26 @@ __device__ __forceinline__ void tc_split2(float x0, float x1, uint32_t& hi, uint
     lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-// 8-byte asynchronous global -> shared copy; src_bytes = 0 writes zeros
-__device__ __forceinline__ void tc_cp8(void* dst, const void* src, int src_bytes) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(tc_smem(dst)), "l"(src), "r"(src_bytes)
-                 : "memory");
+// hi/lo planes of 8 values into row `row`, samples kb..kb+7, of a KR M tile
+__device__ __forceinline__ void tc_store8(unsigned char* hi_plane, unsigned char* lo_plane, int row, int kb,
+                                          const float (&x)[8]) {
+    uint4 hw, lw;
+    tc_split2(x[0], x[1], hw.x, lw.x);
+    tc_split2(x[2], x[3], hw.y, lw.y);
+    tc_split2(x[4], x[5], hw.z, lw.z);
+    tc_split2(x[6], x[7], hw.w, lw.w);
+    *reinterpret_cast<uint4*>(hi_plane + tc_off(row, kb)) = hw;
+    *reinterpret_cast<uint4*>(lo_plane + tc_off(row, kb)) = lw;
 }
 
-// Prefetch the samples of chunk `ch` (region samples [32 ch, 32 ch + 32)) into zs.
-__device__ __forceinline__ void tc_prefetch(const TcArgs& a, cfloat* zs, int ch, int rr0, int cc0, int tid) {
-    const int n = a.n;
-    const int k0 = ch * kTcKC;
-    for (int e = tid; e < kTcKC * n; e += kTcThreads) {
-        const int k = e / n, t = e - k * n;
-        const int sidx = k0 + k;
-        const int ry = sidx / a.region_c, cx = sidx - ry * a.region_c;
-        const int r = rr0 + ry, c = cc0 + cx;
-        const bool in = ry < a.region_r && r < a.rows && c < a.cols;
-        const cfloat* src = in ? a.zt + ((int64_t)r * a.cols + c) * n + t : a.zt;
-        tc_cp8(zs + e, src, in ? 8 : 0);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
+// 8 mask bits -> 8 bf16 (1.0 or 0), packed in pairs (bit 0 -> first element)
+__device__ __forceinline__ uint4 tc_expand8(uint32_t b) {
+    uint4 r;
+    r.x = ((b & 1u) ? 0x3F80u : 0u) | ((b & 2u) ? 0x3F800000u : 0u);
+    r.y = ((b & 4u) ? 0x3F80u : 0u) | ((b & 8u) ? 0x3F800000u : 0u);
+    r.z = ((b & 16u) ? 0x3F80u : 0u) | ((b & 32u) ? 0x3F800000u : 0u);
+    r.w = ((b & 64u) ? 0x3F80u : 0u) | ((b & 128u) ? 0x3F800000u : 0u);
+    return r;
 }
 
 __device__ __forceinline__ void tc_ld32(uint32_t addr, uint32_t (&r)[32]) {
@@ -152,20 +151,39 @@ __device__ __forceinline__ void tc_ld32(uint32_t addr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Prefetch the samples of chunk `ch` into zs[k][t] (builder threads; soff = element
+// offset of each region sample in zt, or -1 outside the image: zero-filled).
+__device__ __forceinline__ void tc_prefetch(const TcArgs& a, cfloat* zs, const int* soff, int ch, int btid) {
+    const int n = a.n;
+    for (int idx = btid; idx < kTcKC * 16; idx += kTcBuilders) {
+        const int k = idx >> 4;
+        const int off = soff[ch * kTcKC + k];
+        for (int t = idx & 15; t < n; t += 16) {
+            const cfloat* src = off >= 0 ? a.zt + off + t : a.zt;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(tc_smem(zs + k * n + t)), "l"(src),
+                         "r"(off >= 0 ? 8 : 0)
+                         : "memory");
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     extern __shared__ unsigned char tc_raw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n = a.n, nn = n * n, wy = 2 * a.hy + 1, wx = 2 * a.hx + 1;
     const int O = n * (n - 1) / 2;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [0], [1]: stage MMA done
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [2] builders -> issuer
+    uint64_t* empty = full + 2;                                      // [2] MMAs done -> builders
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + a.off_bar + 64);
+    int* sfail = reinterpret_cast<int*>(sm + a.off_bar + 72);
     cfloat* const zb0 = reinterpret_cast<cfloat*>(sm + a.off_z);
     cfloat* const zb1 = reinterpret_cast<cfloat*>(sm + a.off_z + a.z_bytes);
-    float* rtab = reinterpret_cast<float*>(sm + a.off_r);           // [128][ld_r]: 1/sqrt(amp_i)
-    uint32_t* pairs = reinterpret_cast<uint32_t*>(sm + a.off_pair); // [O]: i | j << 16
-    uint32_t* mask = reinterpret_cast<uint32_t*>(sm + a.off_mask);  // [128][wy][2]
-    int* win = reinterpret_cast<int*>(sm + a.off_win);              // [128][2]: window origin in region
+    float* rtab = reinterpret_cast<float*>(sm + a.off_r);             // [256][ld_r]: 1/sqrt(amp_i)
+    uint32_t* pbits = reinterpret_cast<uint32_t*>(sm + a.off_pbits);  // [256][kwords]: pixel mask bits
+    int* soff = reinterpret_cast<int*>(sm + a.off_soff);              // [kpad]: sample offsets in zt
+    uint32_t* pairs = reinterpret_cast<uint32_t*>(sm + a.off_pair);   // [O]: i | j << 16
 
     for (int o = tid; o < O; o += kTcThreads) {
         int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j, 0 <= j < i
@@ -174,134 +192,123 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
         pairs[o] = (uint32_t)i | ((uint32_t)(o - i * (i - 1) / 2) << 16);
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&bars[0])), "r"(1));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&bars[1])), "r"(1));
+        for (int s = 0; s < 2; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&full[s])), "r"(kTcBuilders / 32));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&empty[s])), "r"(1));
+        }
+        *sfail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    constexpr int kAlloc = kTcMaxPW;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
-                     "r"(kAlloc));
+                     "r"(kTcCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    uint32_t phase[2] = {0u, 0u};
-    uint32_t uses[2] = {0u, 0u};  // commits issued per stage (to know what to wait for)
-    bool failed = false;
+    const bool builder = warp < kTcBuilders / 32;
+    // per-stage state as bit s: mbarrier phase parities, and (builders) an MMA commit on
+    // empty[s] still to be consumed
+    uint32_t ph_full = 0u, ph_empty = 0u, pend = 0u;
     const int nchunks = a.kpad / kTcKC;
 
     const int ntiles = a.tiles_r * a.tiles_c;
-    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int tr0 = (tile / a.tiles_c) * kTcTileR, tc0 = (tile % a.tiles_c) * kTcTileC;
         // region origin: clamped window start of the tile's first output pixel
         const int rr0 = min(max(a.sy / 2 + tr0 * a.sy - a.hy, 0), a.rows - wy);
         const int cc0 = min(max(a.sx / 2 + tc0 * a.sx - a.hx, 0), a.cols - wx);
-        // per-pixel window origin (in region coordinates) and mask bits
-        if (tid < kTcM) {
+        // sample offsets of the region
+        for (int s = tid; s < a.kpad; s += kTcThreads) {
+            const int ry = s / a.region_c, cx = s - ry * a.region_c;
+            const int r = rr0 + ry, c = cc0 + cx;
+            soff[s] = (ry < a.region_r && r < a.rows && c < a.cols) ? (r * a.cols + c) * n : -1;
+        }
+        // per-pixel mask bits over the region's samples
+        if (tid < kTcN) {
+            uint32_t* pb = pbits + tid * a.kwords;
+            for (int w = 0; w < a.kwords; ++w) pb[w] = 0u;
             const int pr = tr0 + tid / kTcTileC, pc = tc0 + tid % kTcTileC;
-            const bool ok = pr < a.out_rows && pc < a.out_cols;
-            int cnt = 0;
-            if (ok) {
+            if (pr < a.out_rows && pc < a.out_cols) {
                 const int r0 = min(max(a.sy / 2 + pr * a.sy - a.hy, 0), a.rows - wy);
                 const int c0 = min(max(a.sx / 2 + pc * a.sx - a.hx, 0), a.cols - wx);
-                win[2 * tid] = r0 - rr0;
-                win[2 * tid + 1] = c0 - cc0;
+                const int wr = r0 - rr0, wc = c0 - cc0;
                 const int64_t p = (int64_t)pr * a.out_cols + pc;
-                const uint64_t full = wx >= 64 ? ~0ull : ((1ull << wx) - 1ull);
-                for (int r = 0; r < wy; ++r) {
-                    uint64_t m = full;
+                const uint64_t fullrow = wx >= 64 ? ~0ull : ((1ull << wx) - 1ull);
+                int cnt = 0;
+                for (int dr = 0; dr < wy; ++dr) {
+                    uint64_t m = fullrow;
                     if (a.bits) {
-                        const uint32_t* w = a.bits + (p * wy + r) * a.wpr;
-                        m = w[0] | (a.wpr > 1 ? (uint64_t)w[1] << 32 : 0ull);
-                        m &= full;
+                        const uint32_t* w = a.bits + (p * wy + dr) * a.wpr;
+                        m = (w[0] | (a.wpr > 1 ? (uint64_t)w[1] << 32 : 0ull)) & fullrow;
                     } else if (a.nb_u8) {
-                        const uint8_t* b = a.nb_u8 + (p * wy + r) * wx;
+                        const uint8_t* b = a.nb_u8 + (p * wy + dr) * wx;
                         m = 0;
                         for (int q = 0; q < wx; ++q) m |= (uint64_t)(b[q] != 0) << q;
                     }
-                    mask[(tid * wy + r) * 2] = (uint32_t)m;
-                    mask[(tid * wy + r) * 2 + 1] = (uint32_t)(m >> 32);
                     cnt += __popcll(m);
+                    const int s0 = (wr + dr) * a.region_c + wc;  // first sample of the window row
+                    const int w0 = s0 >> 5, sh = s0 & 31;
+                    const uint64_t lo = m << sh;
+                    pb[w0] |= (uint32_t)lo;
+                    if ((uint32_t)(lo >> 32)) pb[w0 + 1] |= (uint32_t)(lo >> 32);
+                    const uint32_t hi = sh ? (uint32_t)(m >> (64 - sh)) : 0u;
+                    if (hi) pb[w0 + 2] |= hi;
                 }
                 if (a.counts) a.counts[p] = cnt;
-            } else {
-                win[2 * tid] = -100000;  // never inside
-                win[2 * tid + 1] = -100000;
             }
         }
-        for (int pass = 0; pass < a.npass && !failed; ++pass) {
-            const int pp0 = a.pair0[pass], npairs = a.pair0[pass + 1] - pp0;
-            const int ndiag = pass == 0 ? n : 0;
-            const int pcols = a.pcols[pass];
-            const int gbase = pass == 0 ? 0 : n + 2 * pp0;  // output column of TMEM column 0
-            const int gend = ndiag + 2 * npairs;            // TMEM columns holding outputs
-            tc_prefetch(a, zb0, 0, rr0, cc0, tid);
-            for (int ch = 0; ch < nchunks; ++ch) {
-                const int s = ch & 1;
-                unsigned char* sA = sm + a.off_stage + s * a.stage_bytes;
-                unsigned char* sBh = sA + a.stage_a_bytes;
-                unsigned char* sBl = sBh + a.plane_bytes;
-                // wait until the MMAs that last read this stage are done
-                if (uses[s] > 0) {
-                    if (!tc_wait(&bars[s], phase[s])) failed = true;
-                    phase[s] ^= 1u;
-                    uses[s] = 0;
-                }
-                asm volatile("cp.async.wait_group 0;" ::: "memory");
-                if (__syncthreads_or(failed)) {
-                    failed = true;
-                    break;
-                }
-                if (ch + 1 < nchunks) tc_prefetch(a, (ch & 1) ? zb0 : zb1, ch + 1, rr0, cc0, tid);
-                const cfloat* zs = (ch & 1) ? zb1 : zb0;
-                const int k0 = ch * kTcKC;
-                // A: thread -> (pixel row, 8 samples)
-                {
-                    const int row = tid >> 2, g = tid & 3;
-                    const int wr = win[2 * row], wc = win[2 * row + 1];
-                    const int s0 = k0 + 8 * g;
-                    int ry = s0 / a.region_c, cx = s0 - ry * a.region_c;
-                    uint32_t w4[4];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const int dr = ry - wr, dc = cx - wc;
-                        uint32_t bit = 0u;
-                        if (dr >= 0 && dr < wy && dc >= 0 && dc < wx && ry < a.region_r)
-                            bit = (mask[(row * wy + dr) * 2 + (dc >> 5)] >> (dc & 31)) & 1u;
-                        const uint32_t hv = bit ? 0x3F80u : 0u;  // bf16 1.0 or 0
-                        if (q & 1) w4[q >> 1] |= hv << 16;
-                        else w4[q >> 1] = hv;
-                        if (++cx == a.region_c) {
-                            cx = 0;
-                            ++ry;
-                        }
+        __syncthreads();
+        for (int pass = 0; pass < a.npass; ++pass) {
+            const int e0 = pass * 2 * kTcM;
+            const int e1 = min(e0 + 2 * kTcM, nn);
+            const int mt = e1 - e0 > kTcM ? 2 : 1;  // M tiles holding components
+            // units: diagonal components [dlo, dhi), pairs [plo, phi) meeting [e0, e1)
+            const int dlo = min(e0, n), dhi = min(e1, n);
+            const int plo = (max(e0, n) - n) >> 1;
+            const int phi = e1 > n ? (e1 - n + 1) >> 1 : plo;
+            const int nd = dhi - dlo, units = nd + (phi - plo);
+            if (builder) {
+                const int btid = tid;
+                tc_prefetch(a, zb0, soff, 0, btid);
+                for (int ch = 0; ch < nchunks; ++ch) {
+                    const int s = ch & 1;
+                    unsigned char* stage = sm + a.off_stage + s * kTcStageBytes;
+                    unsigned char* msk = stage + 4 * 8192;
+                    // wait until the MMAs that last read this stage are done
+                    if ((pend >> s) & 1u) {
+                        if (!tc_wait(&empty[s], (ph_empty >> s) & 1u)) atomicExch(sfail, 1);
+                        ph_empty ^= 1u << s;
+                        pend &= ~(1u << s);
                     }
-                    *reinterpret_cast<uint4*>(sA + tc_off(row, 8 * g)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
-                }
-                // B: tasks (diagonal i or pair o) x (8 samples), sample group outermost so
-                // that a warp reads one group of samples
-                {
-                    const int units = ndiag + npairs;
-                    for (int t = tid; t < 4 * units; t += kTcThreads) {
+                    asm volatile("cp.async.wait_group 0;" ::: "memory");
+                    asm volatile("bar.sync 1, %0;" ::"n"(kTcBuilders) : "memory");
+                    if (*(volatile int*)sfail) break;
+                    if (ch + 1 < nchunks) tc_prefetch(a, (ch & 1) ? zb0 : zb1, soff, ch + 1, btid);
+                    const cfloat* zs = (ch & 1) ? zb1 : zb0;
+                    // mask operand: pixel row x 16 samples per task
+                    for (int t = btid; t < 2 * kTcN; t += kTcBuilders) {
+                        const int row = t >> 1, half = t & 1;
+                        const uint32_t b = pbits[row * a.kwords + ch] >> (16 * half);
+                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(b);
+                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(b >> 8);
+                    }
+                    // KR rows: unit (diagonal i or pair o) x 8 samples per task
+                    for (int t = btid; t < 4 * units; t += kTcBuilders) {
                         const int g = t / units, u = t - g * units;
                         const int kb = 8 * g;
-                        uint4 hw, lw;
-                        if (u < ndiag) {
+                        if (u < nd) {
+                            const int i = dlo + u, e = i - e0;
                             float x[8];
 #pragma unroll
-                            for (int q = 0; q < 8; ++q) x[q] = cabs2(zs[(kb + q) * n + u]);
-                            tc_split2(x[0], x[1], hw.x, lw.x);
-                            tc_split2(x[2], x[3], hw.y, lw.y);
-                            tc_split2(x[4], x[5], hw.z, lw.z);
-                            tc_split2(x[6], x[7], hw.w, lw.w);
-                            *reinterpret_cast<uint4*>(sBh + tc_off(u, kb)) = hw;
-                            *reinterpret_cast<uint4*>(sBl + tc_off(u, kb)) = lw;
+                            for (int q = 0; q < 8; ++q) x[q] = cabs2(zs[(kb + q) * n + i]);
+                            unsigned char* hp = stage + (e >> 7) * 16384;
+                            tc_store8(hp, hp + 8192, e & 127, kb, x);
                         } else {
-                            const int o = u - ndiag;
-                            const uint32_t ij = pairs[pp0 + o];
+                            const int o = plo + u - nd;
+                            const uint32_t ij = pairs[o];
                             const int i = ij & 0xffff, j = ij >> 16;
                             float re[8], im[8];
 #pragma unroll
@@ -310,116 +317,117 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                                 re[q] = fmaf(zi.re, zj.re, zi.im * zj.im);    // Re z_i conj(z_j)
                                 im[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
                             }
-                            const int col = ndiag + 2 * o;
-                            tc_split2(re[0], re[1], hw.x, lw.x);
-                            tc_split2(re[2], re[3], hw.y, lw.y);
-                            tc_split2(re[4], re[5], hw.z, lw.z);
-                            tc_split2(re[6], re[7], hw.w, lw.w);
-                            *reinterpret_cast<uint4*>(sBh + tc_off(col, kb)) = hw;
-                            *reinterpret_cast<uint4*>(sBl + tc_off(col, kb)) = lw;
-                            tc_split2(im[0], im[1], hw.x, lw.x);
-                            tc_split2(im[2], im[3], hw.y, lw.y);
-                            tc_split2(im[4], im[5], hw.z, lw.z);
-                            tc_split2(im[6], im[7], hw.w, lw.w);
-                            *reinterpret_cast<uint4*>(sBh + tc_off(col + 1, kb)) = hw;
-                            *reinterpret_cast<uint4*>(sBl + tc_off(col + 1, kb)) = lw;
+                            const int er = n + 2 * o;
+                            if (er >= e0 && er < e1) {
+                                unsigned char* hp = stage + ((er - e0) >> 7) * 16384;
+                                tc_store8(hp, hp + 8192, (er - e0) & 127, kb, re);
+                            }
+                            if (er + 1 >= e0 && er + 1 < e1) {
+                                unsigned char* hp = stage + ((er + 1 - e0) >> 7) * 16384;
+                                tc_store8(hp, hp + 8192, (er + 1 - e0) & 127, kb, im);
+                            }
                         }
                     }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0)
+                        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(
+                                         tc_smem(&full[s]))
+                                     : "memory");
+                    pend |= 1u << s;
                 }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncthreads();
-                if (tid == 0) {
+                // drain: the last MMAs of the pass must be complete before the epilogue
+                for (int s2 = 0; s2 < 2; ++s2) {
+                    if ((pend >> s2) & 1u) {
+                        if (!tc_wait(&empty[s2], (ph_empty >> s2) & 1u)) atomicExch(sfail, 1);
+                        ph_empty ^= 1u << s2;
+                        pend &= ~(1u << s2);
+                    }
+                }
+            } else if (lane == 0) {
+                // MMA issuer
+                constexpr uint32_t LBO = 128, SBO = kTcKC / 8 * 128;
+                const uint32_t idesc = tc_idesc_bf16(kTcM, kTcN);
+                for (int ch = 0; ch < nchunks; ++ch) {
+                    const int s = ch & 1;
+                    if (!tc_wait(&full[s], (ph_full >> s) & 1u)) {
+                        atomicExch(sfail, 1);
+                        break;
+                    }
+                    ph_full ^= 1u << s;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t a_base = tc_smem(sA), b_hi = tc_smem(sBh), b_lo = tc_smem(sBl);
-                    constexpr uint32_t LBO = 128, SBO = kTcKC / 8 * 128;
-                    for (int kk = 0; kk < kTcKC; kk += 16) {
-                        const uint64_t ad = tc_desc(a_base + (kk / 8) * LBO, LBO, SBO);
-                        for (int n0 = 0; n0 < pcols; n0 += 256) {
-                            const int nw = min(256, pcols - n0);
-                            const uint32_t idesc = tc_idesc_bf16(kTcM, nw);
-                            const uint32_t boff = (uint32_t)(n0 / 8) * SBO + (kk / 8) * LBO;
-                            const uint32_t dt = tmem + (uint32_t)n0;
+                    const uint32_t st = tc_smem(sm + a.off_stage + s * kTcStageBytes);
+                    const uint32_t mk = st + 4 * 8192;
+                    for (int t = 0; t < mt; ++t) {
+                        const uint32_t khi = st + t * 16384, klo = khi + 8192;
+                        const uint32_t dt = tmem + (uint32_t)(t * kTcN);
+                        for (int kk = 0; kk < kTcKC; kk += 16) {
+                            const uint32_t koff = (kk / 8) * LBO;
+                            const uint64_t bd = tc_desc(mk + koff, LBO, SBO);
+                            const uint64_t ah = tc_desc(khi + koff, LBO, SBO);
+                            const uint64_t al = tc_desc(klo + koff, LBO, SBO);
                             const uint32_t acc0 = (ch > 0 || kk > 0) ? 1u : 0u;
-                            const uint64_t bh = tc_desc(b_hi + boff, LBO, SBO);
-                            const uint64_t bl = tc_desc(b_lo + boff, LBO, SBO);
                             asm volatile(
                                 "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
-                                "l"(ad), "l"(bh), "r"(idesc), "r"(acc0));
+                                "l"(ah), "l"(bd), "r"(idesc), "r"(acc0));
                             asm volatile(
                                 "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
-                                "l"(ad), "l"(bl), "r"(idesc), "r"(1u));
+                                "l"(al), "l"(bd), "r"(idesc), "r"(1u));
                         }
                     }
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                     tc_smem(&bars[s]))
+                                     tc_smem(&empty[s]))
                                  : "memory");
                 }
-                uses[s] = 1;
             }
-            if (failed) break;
-            // drain: wait for both stages' last MMAs (the accumulator is then complete)
-            for (int s2 = 0; s2 < 2; ++s2) {
-                if (uses[s2] > 0) {
-                    if (!tc_wait(&bars[s2], phase[s2])) failed = true;
-                    phase[s2] ^= 1u;
-                    uses[s2] = 0;
-                }
-            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            if (__syncthreads_or(failed)) {
-                failed = true;
-                break;
-            }
-            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (pixels) and every
-            // fourth group of 32 columns starting at group w / 4
-            const int quarter = warp & 3, part = warp >> 2;
+            if (*(volatile int*)sfail) break;
+            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (components) for the
+            // 32-pixel groups b = w / 4, w / 4 + 4, ... of each M tile
+            const int quarter = warp & 3;
             const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-            float* tbuf = reinterpret_cast<float*>(sm + a.off_stage) + warp * (32 * 33);
             if (pass == 0) {
-                // the diagonal (|z_i|^2 sums) is columns 0..n-1 of pass 0: r_i = 1 / sqrt(amp_i)
-                if (part == 0) {
-                    for (int c0 = 0; c0 < n; c0 += 32) {
+                // the diagonal (|z_i|^2 sums) is components 0..n-1: r_i = 1 / sqrt(amp_i)
+                if (quarter * 32 < n) {
+                    for (int g = warp >> 2; g < kTcN / 32; g += 4) {
                         uint32_t r[32];
-                        tc_ld32(tmem + lane_base + (uint32_t)c0, r);
-                        float* rrow = rtab + (quarter * 32 + lane) * a.ld_r;
+                        tc_ld32(tmem + lane_base + (uint32_t)(32 * g), r);
+                        const int i = quarter * 32 + lane;
+                        if (i < n) {
 #pragma unroll
-                        for (int q = 0; q < 32; ++q)
-                            if (c0 + q < n) rrow[c0 + q] = 1.f / sqrtf(__uint_as_float(r[q]));
+                            for (int q = 0; q < 32; ++q)
+                                rtab[(32 * g + q) * a.ld_r + i] = 1.f / sqrtf(__uint_as_float(r[q]));
+                        }
                     }
                 }
                 __syncthreads();
             }
-            for (int c0 = 32 * part; c0 < gend; c0 += 32 * 4) {
+            for (int b = warp >> 2; b < mt * (kTcN / 32); b += 4) {
+                const int t = b / (kTcN / 32), g = b % (kTcN / 32);
                 uint32_t r[32];
-                tc_ld32(tmem + lane_base + (uint32_t)c0, r);
-                __syncwarp();
-#pragma unroll
-                for (int q = 0; q < 32; ++q) tbuf[lane * 33 + q] = __uint_as_float(r[q]);
-                __syncwarp();
-                // lane -> column c0 + lane and its (i, j)
-                const int c = c0 + lane;
-                int ci = 0, cj = 0;
-                if (c < gend) {
-                    if (c < ndiag) {
-                        ci = cj = c;
-                    } else {
-                        const uint32_t ij = pairs[pp0 + ((c - ndiag) >> 1)];
+                tc_ld32(tmem + lane_base + (uint32_t)(t * kTcN + 32 * g), r);
+                const int e = e0 + t * kTcM + quarter * 32 + lane;  // this lane's component
+                if (e < e1) {
+                    int ci = e, cj = e;
+                    if (e >= n) {
+                        const uint32_t ij = pairs[(e - n) >> 1];
                         ci = ij & 0xffff;
                         cj = ij >> 16;
                     }
-                }
-                for (int rr = 0; rr < 32; ++rr) {
-                    const int pl = quarter * 32 + rr;
-                    const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
-                    if (pr < a.out_rows && pc < a.out_cols && c < gend) {
-                        const float* rrow = rtab + pl * a.ld_r;
-                        const float f = rrow[ci] * rrow[cj];
-                        const float x = tbuf[rr * 33 + lane];
-                        const int64_t p = (int64_t)pr * a.out_cols + pc;
-                        a.Cg[p * nn + gbase + c] = f < 1e6f ? x * f : 0.f;
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) {
+                        const int pl = 32 * g + q;
+                        const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
+                        if (pr < a.out_rows && pc < a.out_cols) {
+                            const float* rrow = rtab + pl * a.ld_r;
+                            const float f = rrow[ci] * rrow[cj];
+                            const int64_t p = (int64_t)pr * a.out_cols + pc;
+                            a.Cg[p * nn + e] = f < 1e6f ? __uint_as_float(r[q]) * f : 0.f;
+                        }
                     }
                 }
             }
@@ -427,15 +435,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         }
+        if (*(volatile int*)sfail) break;
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
-    if (failed && tid == 0) atomicExch(a.status, (int)DPL_ERR_TIMEOUT);
+    if (tid == 0 && *(volatile int*)sfail) atomicExch(a.status, (int)DPL_ERR_TIMEOUT);
     // before releasing TMEM make sure no MMA is still in flight (bounded)
-    for (int s2 = 0; s2 < 2; ++s2)
-        if (uses[s2] > 0) tc_wait(&bars[s2], phase[s2]);
+    if (builder)
+        for (int s2 = 0; s2 < 2; ++s2)
+            if ((pend >> s2) & 1u) tc_wait(&empty[s2], (ph_empty >> s2) & 1u);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kAlloc));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
 }
 
 }  // namespace dpl

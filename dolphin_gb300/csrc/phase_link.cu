@@ -551,36 +551,16 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
     a.out_cols = cols / sx;
     const int wy = 2 * hy + 1, wx = 2 * hx + 1;
     if (wx > 64 || n < 1 || n > 64) return false;
-    a.tile_r = kTcTileR;
-    a.tile_c = kTcTileC;
-    a.tiles_r = ceil_div(std::max(a.out_rows, 1), a.tile_r);
-    a.tiles_c = ceil_div(std::max(a.out_cols, 1), a.tile_c);
-    a.region_r = (a.tile_r - 1) * sy + wy;
-    a.region_c = (a.tile_c - 1) * sx + wx;
+    if ((int64_t)rows * cols * n >= (int64_t)1 << 31) return false;  // 32-bit sample offsets
+    a.tiles_r = ceil_div(std::max(a.out_rows, 1), kTcTileR);
+    a.tiles_c = ceil_div(std::max(a.out_cols, 1), kTcTileC);
+    a.region_r = (kTcTileR - 1) * sy + wy;
+    a.region_c = (kTcTileC - 1) * sx + wx;
     a.kpad = (int)(ceil_div((int64_t)a.region_r * a.region_c, kTcKC) * kTcKC);
-    // passes of <= 512 TMEM columns split at pair boundaries, pass 0 with the diagonal
-    const int O = n * (n - 1) / 2;
-    bool ok = false;
-    for (a.npass = std::max(1, ceil_div(n * n, kTcMaxPW)); a.npass <= kTcMaxPass && !ok; ++a.npass) {
-        const int target = ceil_div(n * n, a.npass);
-        int o = 0;
-        ok = true;
-        a.pair0[0] = 0;
-        for (int p = 0; p < a.npass; ++p) {
-            const int base = p == 0 ? n : 0;
-            const int cnt = p == a.npass - 1 ? O - o : std::min(O - o, std::max(0, (target - base) / 2));
-            const int cols_p = std::max(16, ceil_div(base + 2 * cnt, 16) * 16);
-            if (cols_p > kTcMaxPW) ok = false;
-            a.pcols[p] = cols_p;
-            o += cnt;
-            a.pair0[p + 1] = o;
-        }
-        if (ok) break;
-    }
-    if (!ok) return false;
-    int pw_max = 0;
-    for (int p = 0; p < a.npass; ++p) pw_max = std::max(pw_max, a.pcols[p]);
+    a.kwords = a.kpad / 32;
+    a.npass = ceil_div(n * n, 2 * kTcM);
     a.ld_r = n | 1;
+    const int O = n * (n - 1) / 2;
     size_t o = 0;
     auto take = [&](size_t bytes, size_t al) {
         o = align_up(o, al);
@@ -588,16 +568,13 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
         o += bytes;
         return (int)at;
     };
-    a.stage_a_bytes = kTcM * kTcKC * 2;
-    a.plane_bytes = pw_max * kTcKC * 2;
-    a.stage_bytes = (int)align_up((size_t)a.stage_a_bytes + 2 * (size_t)a.plane_bytes, 1024);
-    a.off_stage = take(std::max((size_t)2 * a.stage_bytes, (size_t)kTcTbufBytes), 1024);
+    a.off_stage = take(2 * (size_t)kTcStageBytes, 1024);
     a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
     a.off_z = take(2 * (size_t)a.z_bytes, 16);
-    a.off_r = take((size_t)kTcM * a.ld_r * sizeof(float), 16);
+    a.off_r = take((size_t)kTcN * a.ld_r * sizeof(float), 16);
+    a.off_pbits = take((size_t)kTcN * a.kwords * sizeof(uint32_t), 16);
+    a.off_soff = take((size_t)a.kpad * sizeof(int), 16);
     a.off_pair = take((size_t)std::max(O, 1) * sizeof(uint32_t), 16);
-    a.off_mask = take((size_t)kTcM * wy * 2 * sizeof(uint32_t), 16);
-    a.off_win = take((size_t)kTcM * 2 * sizeof(int), 16);
     a.off_bar = take(128, 64);
     a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
     return a.smem_bytes <= 227 * 1024;
