@@ -62,8 +62,10 @@ struct TcArgs {
     int32_t* counts;         // (out_rows * out_cols) or null
     int* status;
     // shared-memory carve (bytes from the 1024-aligned base)
-    int off_stage, off_z, z_bytes, off_r, off_pbits, off_soff, off_pair, off_bar, smem_bytes;
+    int off_stage, off_z, z_bytes, off_r, off_pbits, off_soff, off_runs, off_pair, off_bar, smem_bytes;
 };
+
+constexpr int kTcRuns = 3;  // contiguous runs of image samples per K chunk (a chunk spans <= 3 region rows)
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = 0;
@@ -168,6 +170,41 @@ __device__ __forceinline__ void tc_prefetch(const TcArgs& a, cfloat* zs, const i
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
+// Even N: the chunk's image samples are <= 3 contiguous runs of zt (one per region
+// row); thread 0 copies them with 1-D bulk copies that complete on zbar, and the
+// builders zero the chunk's samples outside the image.  runs[ch][r] = (k_start |
+// len << 8, element offset) with len = 0 for an unused slot.
+__device__ __forceinline__ void tc_prefetch_bulk(const TcArgs& a, cfloat* zs, uint64_t* zbar, const int* soff,
+                                                 const int2* runs, int ch, int btid) {
+    const int n = a.n;
+    if (btid == 0) {
+        const int2* rc = runs + ch * kTcRuns;
+        uint32_t total = 0;
+#pragma unroll
+        for (int r = 0; r < kTcRuns; ++r) total += (uint32_t)((rc[r].x >> 8) * n * 8);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                         tc_smem(zbar)),
+                     "r"(total)
+                     : "memory");
+#pragma unroll
+        for (int r = 0; r < kTcRuns; ++r) {
+            const int len = rc[r].x >> 8;
+            if (len > 0)
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        tc_smem(zs + (rc[r].x & 0xff) * n)),
+                    "l"(a.zt + rc[r].y), "r"(len * n * 8), "r"(tc_smem(zbar))
+                    : "memory");
+        }
+    }
+    for (int idx = btid; idx < kTcKC * 16; idx += kTcBuilders) {
+        const int k = idx >> 4;
+        if (soff[ch * kTcKC + k] < 0)
+            for (int t = idx & 15; t < n; t += 16) zs[k * n + t] = cmake(0.f, 0.f);
+    }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     extern __shared__ unsigned char tc_raw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
@@ -176,8 +213,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     const int O = n * (n - 1) / 2;
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [2] builders -> issuer
     uint64_t* empty = full + 2;                                      // [2] MMAs done -> builders
+    uint64_t* zbar = full + 4;                                       // [2] bulk sample copies landed
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + a.off_bar + 64);
     int* sfail = reinterpret_cast<int*>(sm + a.off_bar + 72);
+    int2* runs = reinterpret_cast<int2*>(sm + a.off_runs);          // [nchunks][kTcRuns]
+    const bool bulk = (a.n & 1) == 0;
     cfloat* const zb0 = reinterpret_cast<cfloat*>(sm + a.off_z);
     cfloat* const zb1 = reinterpret_cast<cfloat*>(sm + a.off_z + a.z_bytes);
     float* rtab = reinterpret_cast<float*>(sm + a.off_r);             // [256][ld_r]: 1/sqrt(amp_i)
@@ -195,6 +235,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
         for (int s = 0; s < 2; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&full[s])), "r"(kTcBuilders / 32));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&empty[s])), "r"(1));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&zbar[s])), "r"(1));
         }
         *sfail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -211,7 +252,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     const bool builder = warp < kTcBuilders / 32;
     // per-stage state as bit s: mbarrier phase parities, and (builders) an MMA commit on
     // empty[s] still to be consumed
-    uint32_t ph_full = 0u, ph_empty = 0u, pend = 0u;
+    uint32_t ph_full = 0u, ph_empty = 0u, pend = 0u, ph_z = 0u;
     const int nchunks = a.kpad / kTcKC;
 
     const int ntiles = a.tiles_r * a.tiles_c;
@@ -225,6 +266,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             const int ry = s / a.region_c, cx = s - ry * a.region_c;
             const int r = rr0 + ry, c = cc0 + cx;
             soff[s] = (ry < a.region_r && r < a.rows && c < a.cols) ? (r * a.cols + c) * n : -1;
+        }
+        __syncthreads();
+        if (bulk) {
+            for (int ch = tid; ch < nchunks; ch += kTcThreads) {
+                int2* rc = runs + ch * kTcRuns;
+                int nr = 0;
+                for (int k = 0; k < kTcKC;) {
+                    const int off = soff[ch * kTcKC + k];
+                    if (off < 0) {
+                        ++k;
+                        continue;
+                    }
+                    int len = 1;
+                    while (k + len < kTcKC && soff[ch * kTcKC + k + len] == off + len * n) ++len;
+                    if (nr < kTcRuns) rc[nr++] = make_int2(k | (len << 8), off);
+                    k += len;
+                }
+                for (; nr < kTcRuns; ++nr) rc[nr] = make_int2(0, 0);
+            }
         }
         // per-pixel mask bits over the region's samples
         if (tid < kTcN) {
@@ -272,7 +332,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             const int nd = dhi - dlo, units = nd + (phi - plo);
             if (builder) {
                 const int btid = tid;
-                tc_prefetch(a, zb0, soff, 0, btid);
+                if (bulk) tc_prefetch_bulk(a, zb0, &zbar[0], soff, runs, 0, btid);
+                else tc_prefetch(a, zb0, soff, 0, btid);
                 for (int ch = 0; ch < nchunks; ++ch) {
                     const int s = ch & 1;
                     unsigned char* stage = sm + a.off_stage + s * kTcStageBytes;
@@ -283,10 +344,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                         ph_empty ^= 1u << s;
                         pend &= ~(1u << s);
                     }
-                    asm volatile("cp.async.wait_group 0;" ::: "memory");
+                    if (bulk) {
+                        if (!tc_wait(&zbar[s], (ph_z >> s) & 1u)) atomicExch(sfail, 1);
+                        ph_z ^= 1u << s;
+                    } else {
+                        asm volatile("cp.async.wait_group 0;" ::: "memory");
+                    }
                     asm volatile("bar.sync 1, %0;" ::"n"(kTcBuilders) : "memory");
                     if (*(volatile int*)sfail) break;
-                    if (ch + 1 < nchunks) tc_prefetch(a, (ch & 1) ? zb0 : zb1, soff, ch + 1, btid);
+                    if (ch + 1 < nchunks) {
+                        if (bulk) tc_prefetch_bulk(a, (ch & 1) ? zb0 : zb1, &zbar[(ch + 1) & 1], soff, runs, ch + 1, btid);
+                        else tc_prefetch(a, (ch & 1) ? zb0 : zb1, soff, ch + 1, btid);
+                    }
                     const cfloat* zs = (ch & 1) ? zb1 : zb0;
                     // mask operand: pixel row x 16 samples per task
                     for (int t = btid; t < 2 * kTcN; t += kTcBuilders) {
@@ -297,7 +366,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                     }
                     // KR rows: unit (diagonal i or pair o) x 8 samples per task
                     for (int t = btid; t < 4 * units; t += kTcBuilders) {
-                        const int g = t / units, u = t - g * units;
+                        const int g = (t >= units) + (t >= 2 * units) + (t >= 3 * units), u = t - g * units;
                         const int kb = 8 * g;
                         if (u < nd) {
                             const int i = dlo + u, e = i - e0;

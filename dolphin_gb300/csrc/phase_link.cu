@@ -574,6 +574,7 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
     a.off_r = take((size_t)kTcN * a.ld_r * sizeof(float), 16);
     a.off_pbits = take((size_t)kTcN * a.kwords * sizeof(uint32_t), 16);
     a.off_soff = take((size_t)a.kpad * sizeof(int), 16);
+    a.off_runs = take((size_t)(a.kpad / kTcKC) * kTcRuns * sizeof(int2), 16);
     a.off_pair = take((size_t)std::max(O, 1) * sizeof(uint32_t), 16);
     a.off_bar = take(128, 64);
     a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
