@@ -207,7 +207,9 @@ __device__ __forceinline__ void tc_prefetch_bulk(const TcArgs& a, cfloat* zs, ui
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     extern __shared__ unsigned char tc_raw[];
-    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
+    // 1024-byte aligned base, derived from the shared array itself so that every access
+    // below stays a shared-memory access
+    unsigned char* sm = tc_raw + ((1024u - (tc_smem(tc_raw) & 1023u)) & 1023u);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n = a.n, nn = n * n, wy = 2 * a.hy + 1, wx = 2 * a.hx + 1;
     const int O = n * (n - 1) / 2;
@@ -338,14 +340,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                     const int s = ch & 1;
                     unsigned char* stage = sm + a.off_stage + s * kTcStageBytes;
                     unsigned char* msk = stage + 4 * 8192;
-                    // wait until the MMAs that last read this stage are done
+                    // thread 0 waits until the MMAs that last read this stage are done and
+                    // (even N) the chunk's samples have landed; the named barrier then
+                    // releases every builder
                     if ((pend >> s) & 1u) {
-                        if (!tc_wait(&empty[s], (ph_empty >> s) & 1u)) atomicExch(sfail, 1);
+                        if (btid == 0 && !tc_wait(&empty[s], (ph_empty >> s) & 1u)) atomicExch(sfail, 1);
                         ph_empty ^= 1u << s;
                         pend &= ~(1u << s);
                     }
                     if (bulk) {
-                        if (!tc_wait(&zbar[s], (ph_z >> s) & 1u)) atomicExch(sfail, 1);
+                        if (btid == 0 && !tc_wait(&zbar[s], (ph_z >> s) & 1u)) atomicExch(sfail, 1);
                         ph_z ^= 1u << s;
                     } else {
                         asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 // drain: the last MMAs of the pass must be complete before the epilogue
                 for (int s2 = 0; s2 < 2; ++s2) {
                     if ((pend >> s2) & 1u) {
-                        if (!tc_wait(&empty[s2], (ph_empty >> s2) & 1u)) atomicExch(sfail, 1);
+                        if (btid == 0 && !tc_wait(&empty[s2], (ph_empty >> s2) & 1u)) atomicExch(sfail, 1);
                         ph_empty ^= 1u << s2;
                         pend &= ~(1u << s2);
                     }
@@ -509,7 +513,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     if (tid == 0 && *(volatile int*)sfail) atomicExch(a.status, (int)DPL_ERR_TIMEOUT);
     // before releasing TMEM make sure no MMA is still in flight (bounded)
-    if (builder)
+    if (tid == 0)
         for (int s2 = 0; s2 < 2; ++s2)
             if ((pend >> s2) & 1u) tc_wait(&empty[s2], (ph_empty >> s2) & 1u);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -87,7 +87,10 @@ template <bool kBits>
 __global__ void __launch_bounds__(256) k_glrt(const __grid_constant__ CUtensorMap tmap, GlrtArgs a) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
-    float* raw = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    // 128-byte aligned base (TMA destination), offset within the shared array so that
+    // the accesses below stay shared-memory accesses
+    const uint32_t mis = (uint32_t)__cvta_generic_to_shared(smem_raw) & 127u;
+    float* raw = reinterpret_cast<float*>(smem_raw + ((128u - mis) & 127u));
     const int n_tile = a.box_w * a.box_h;
     float* lg = raw + n_tile;
     const int wy = 2 * a.hy + 1, wx = 2 * a.hx + 1;
