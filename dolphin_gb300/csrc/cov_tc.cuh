@@ -45,7 +45,7 @@ constexpr int kTcThreads = 512;              // 16 warps
 constexpr int kTcBuilders = 480;             // warps 0-14; warp 15 issues the MMAs
 constexpr int kTcCols = 512;                 // TMEM columns: two M tiles x 256 pixels
 constexpr int kTcStageBytes = 4 * 8192 + 16384;  // KR hi/lo of two M tiles + mask
-constexpr uint32_t kTcWaitLimit = 1u << 26;
+constexpr uint32_t kTcWaitLimit = 1u << 25;  // polls (>= 64 ns apart): a few seconds
 
 struct TcArgs {
     int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
@@ -98,10 +98,13 @@ __device__ __forceinline__ bool tc_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// bounded wait; returns false on timeout
+// bounded wait with a short sleep between polls (a spinning thread would take issue
+// slots from the warps it waits for); returns false on timeout
 __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t it = 0; it < kTcWaitLimit; ++it)
+    for (uint32_t it = 0; it < kTcWaitLimit; ++it) {
         if (tc_try_wait(bar, parity)) return true;
+        __nanosleep(64);
+    }
     return false;
 }
 
@@ -119,16 +122,14 @@ __device__ __forceinline__ void tc_split2(float x0, float x1, uint32_t& hi, uint
     lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-// hi/lo planes of 8 values into row `row`, samples kb..kb+7, of a KR M tile
-__device__ __forceinline__ void tc_store8(unsigned char* hi_plane, unsigned char* lo_plane, int row, int kb,
-                                          const float (&x)[8]) {
-    uint4 hw, lw;
+// hi/lo planes of 4 values into row `row`, samples kb..kb+3 (kb a multiple of 4)
+__device__ __forceinline__ void tc_store4(unsigned char* hi_plane, unsigned char* lo_plane, int row, int kb,
+                                          const float (&x)[4]) {
+    uint2 hw, lw;
     tc_split2(x[0], x[1], hw.x, lw.x);
     tc_split2(x[2], x[3], hw.y, lw.y);
-    tc_split2(x[4], x[5], hw.z, lw.z);
-    tc_split2(x[6], x[7], hw.w, lw.w);
-    *reinterpret_cast<uint4*>(hi_plane + tc_off(row, kb)) = hw;
-    *reinterpret_cast<uint4*>(lo_plane + tc_off(row, kb)) = lw;
+    *reinterpret_cast<uint2*>(hi_plane + tc_off(row, kb)) = hw;
+    *reinterpret_cast<uint2*>(lo_plane + tc_off(row, kb)) = lw;
 }
 
 // 8 mask bits -> 8 bf16 (1.0 or 0), packed in pairs (bit 0 -> first element)
@@ -361,43 +362,58 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                         else tc_prefetch(a, (ch & 1) ? zb0 : zb1, soff, ch + 1, btid);
                     }
                     const cfloat* zs = (ch & 1) ? zb1 : zb0;
-                    // mask operand: pixel row x 16 samples per task
-                    for (int t = btid; t < 2 * kTcN; t += kTcBuilders) {
-                        const int row = t >> 1, half = t & 1;
-                        const uint32_t b = pbits[row * a.kwords + ch] >> (16 * half);
-                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(b);
-                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(b >> 8);
-                    }
-                    // KR rows: unit (diagonal i or pair o) x 8 samples per task
-                    for (int t = btid; t < 4 * units; t += kTcBuilders) {
-                        const int g = (t >= units) + (t >= 2 * units) + (t >= 3 * units), u = t - g * units;
-                        const int kb = 8 * g;
+                    // one striped work list so that every builder does about the same:
+                    // KR items (unit = diagonal i or pair o) x 4 samples, then mask items
+                    // (pixel row x 16 samples)
+                    const int nkr = 8 * units;
+                    for (int t = btid; t < nkr + 2 * kTcN; t += kTcBuilders) {
+                        if (t >= nkr) {
+                            const int m = t - nkr, row = m >> 1, half = m & 1;
+                            const uint32_t b = pbits[row * a.kwords + ch] >> (16 * half);
+                            *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(b);
+                            *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(b >> 8);
+                            continue;
+                        }
+                        int g = 0, u = t;  // g = t / units (g < 8) without a division
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const int step = units << (2 - q);
+                            if (u >= step) {
+                                u -= step;
+                                g += 4 >> q;
+                            }
+                        }
+                        const int kb = 4 * g;
+                        const cfloat* zk = zs + kb * n;  // sample kb; + n per sample
                         if (u < nd) {
                             const int i = dlo + u, e = i - e0;
-                            float x[8];
+                            float x[4];
+                            const cfloat* zi = zk + i;
 #pragma unroll
-                            for (int q = 0; q < 8; ++q) x[q] = cabs2(zs[(kb + q) * n + i]);
+                            for (int q = 0; q < 4; ++q, zi += n) x[q] = cabs2(*zi);
                             unsigned char* hp = stage + (e >> 7) * 16384;
-                            tc_store8(hp, hp + 8192, e & 127, kb, x);
+                            tc_store4(hp, hp + 8192, e & 127, kb, x);
                         } else {
                             const int o = plo + u - nd;
                             const uint32_t ij = pairs[o];
                             const int i = ij & 0xffff, j = ij >> 16;
-                            float re[8], im[8];
+                            float re[4], im[4];
+                            const cfloat* pi = zk + i;
+                            const cfloat* pj = zk + j;
 #pragma unroll
-                            for (int q = 0; q < 8; ++q) {
-                                const cfloat zi = zs[(kb + q) * n + i], zj = zs[(kb + q) * n + j];
+                            for (int q = 0; q < 4; ++q, pi += n, pj += n) {
+                                const cfloat zi = *pi, zj = *pj;
                                 re[q] = fmaf(zi.re, zj.re, zi.im * zj.im);    // Re z_i conj(z_j)
                                 im[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
                             }
                             const int er = n + 2 * o;
                             if (er >= e0 && er < e1) {
                                 unsigned char* hp = stage + ((er - e0) >> 7) * 16384;
-                                tc_store8(hp, hp + 8192, (er - e0) & 127, kb, re);
+                                tc_store4(hp, hp + 8192, (er - e0) & 127, kb, re);
                             }
                             if (er + 1 >= e0 && er + 1 < e1) {
                                 unsigned char* hp = stage + ((er + 1 - e0) >> 7) * 16384;
-                                tc_store8(hp, hp + 8192, (er + 1 - e0) & 127, kb, im);
+                                tc_store4(hp, hp + 8192, (er + 1 - e0) & 127, kb, im);
                             }
                         }
                     }
