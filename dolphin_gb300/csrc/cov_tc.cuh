@@ -66,6 +66,7 @@ struct TcArgs {
 };
 
 constexpr int kTcRuns = 3;  // contiguous runs of image samples per K chunk (a chunk spans <= 3 region rows)
+constexpr int kTcZBuf = 4;  // ring of chunk sample buffers (bulk prefetch distance)
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = 0;
@@ -122,14 +123,16 @@ __device__ __forceinline__ void tc_split2(float x0, float x1, uint32_t& hi, uint
     lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-// hi/lo planes of 4 values into row `row`, samples kb..kb+3 (kb a multiple of 4)
-__device__ __forceinline__ void tc_store4(unsigned char* hi_plane, unsigned char* lo_plane, int row, int kb,
-                                          const float (&x)[4]) {
-    uint2 hw, lw;
+// hi/lo planes of 8 values into row `row`, samples kb..kb+7, of a KR M tile
+__device__ __forceinline__ void tc_store8(unsigned char* hi_plane, unsigned char* lo_plane, int row, int kb,
+                                          const float (&x)[8]) {
+    uint4 hw, lw;
     tc_split2(x[0], x[1], hw.x, lw.x);
     tc_split2(x[2], x[3], hw.y, lw.y);
-    *reinterpret_cast<uint2*>(hi_plane + tc_off(row, kb)) = hw;
-    *reinterpret_cast<uint2*>(lo_plane + tc_off(row, kb)) = lw;
+    tc_split2(x[4], x[5], hw.z, lw.z);
+    tc_split2(x[6], x[7], hw.w, lw.w);
+    *reinterpret_cast<uint4*>(hi_plane + tc_off(row, kb)) = hw;
+    *reinterpret_cast<uint4*>(lo_plane + tc_off(row, kb)) = lw;
 }
 
 // 8 mask bits -> 8 bf16 (1.0 or 0), packed in pairs (bit 0 -> first element)
@@ -172,37 +175,31 @@ __device__ __forceinline__ void tc_prefetch(const TcArgs& a, cfloat* zs, const i
 }
 
 // Even N: the chunk's image samples are <= 3 contiguous runs of zt (one per region
-// row); thread 0 copies them with 1-D bulk copies that complete on zbar, and the
-// builders zero the chunk's samples outside the image.  runs[ch][r] = (k_start |
-// len << 8, element offset) with len = 0 for an unused slot.
-__device__ __forceinline__ void tc_prefetch_bulk(const TcArgs& a, cfloat* zs, uint64_t* zbar, const int* soff,
-                                                 const int2* runs, int ch, int btid) {
+// row), copied by one thread with 1-D bulk copies that complete on zbar.  Samples
+// outside the image are not copied: no pixel's window contains them, so whatever
+// finite values their slots hold are multiplied by zero mask entries.
+// runs[ch][r] = (k_start | len << 8, element offset), len = 0 for an unused slot.
+__device__ __forceinline__ void tc_prefetch_bulk(const TcArgs& a, cfloat* zs, uint64_t* zbar, const int2* runs,
+                                                 int ch) {
     const int n = a.n;
-    if (btid == 0) {
-        const int2* rc = runs + ch * kTcRuns;
-        uint32_t total = 0;
+    const int2* rc = runs + ch * kTcRuns;
+    uint32_t total = 0;
 #pragma unroll
-        for (int r = 0; r < kTcRuns; ++r) total += (uint32_t)((rc[r].x >> 8) * n * 8);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
-                         tc_smem(zbar)),
-                     "r"(total)
-                     : "memory");
+    for (int r = 0; r < kTcRuns; ++r) total += (uint32_t)((rc[r].x >> 8) * n * 8);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     tc_smem(zbar)),
+                 "r"(total)
+                 : "memory");
 #pragma unroll
-        for (int r = 0; r < kTcRuns; ++r) {
-            const int len = rc[r].x >> 8;
-            if (len > 0)
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        tc_smem(zs + (rc[r].x & 0xff) * n)),
-                    "l"(a.zt + rc[r].y), "r"(len * n * 8), "r"(tc_smem(zbar))
-                    : "memory");
-        }
-    }
-    for (int idx = btid; idx < kTcKC * 16; idx += kTcBuilders) {
-        const int k = idx >> 4;
-        if (soff[ch * kTcKC + k] < 0)
-            for (int t = idx & 15; t < n; t += 16) zs[k * n + t] = cmake(0.f, 0.f);
+    for (int r = 0; r < kTcRuns; ++r) {
+        const int len = rc[r].x >> 8;
+        if (len > 0)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    tc_smem(zs + (rc[r].x & 0xff) * n)),
+                "l"(a.zt + rc[r].y), "r"(len * n * 8), "r"(tc_smem(zbar))
+                : "memory");
     }
 }
 
@@ -216,18 +213,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     const int O = n * (n - 1) / 2;
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [2] builders -> issuer
     uint64_t* empty = full + 2;                                      // [2] MMAs done -> builders
-    uint64_t* zbar = full + 4;                                       // [2] bulk sample copies landed
+    uint64_t* zbar = full + 4;                                       // [kTcZBuf] bulk sample copies landed
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + a.off_bar + 64);
     int* sfail = reinterpret_cast<int*>(sm + a.off_bar + 72);
     int2* runs = reinterpret_cast<int2*>(sm + a.off_runs);          // [nchunks][kTcRuns]
     const bool bulk = (a.n & 1) == 0;
-    cfloat* const zb0 = reinterpret_cast<cfloat*>(sm + a.off_z);
-    cfloat* const zb1 = reinterpret_cast<cfloat*>(sm + a.off_z + a.z_bytes);
+    auto zbuf = [&](int c) { return reinterpret_cast<cfloat*>(sm + a.off_z + (c & (kTcZBuf - 1)) * a.z_bytes); };
     float* rtab = reinterpret_cast<float*>(sm + a.off_r);             // [256][ld_r]: 1/sqrt(amp_i)
     uint32_t* pbits = reinterpret_cast<uint32_t*>(sm + a.off_pbits);  // [256][kwords]: pixel mask bits
     int* soff = reinterpret_cast<int*>(sm + a.off_soff);              // [kpad]: sample offsets in zt
     uint32_t* pairs = reinterpret_cast<uint32_t*>(sm + a.off_pair);   // [O]: i | j << 16
 
+    for (int e = tid; e < kTcZBuf * a.z_bytes / 4; e += kTcThreads)  // no NaN patterns in unused slots
+        reinterpret_cast<float*>(sm + a.off_z)[e] = 0.f;
     for (int o = tid; o < O; o += kTcThreads) {
         int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j, 0 <= j < i
         while (i * (i - 1) / 2 > o) --i;
@@ -238,8 +236,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
         for (int s = 0; s < 2; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&full[s])), "r"(kTcBuilders / 32));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&empty[s])), "r"(1));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&zbar[s])), "r"(1));
         }
+        for (int c = 0; c < kTcZBuf; ++c)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&zbar[c])), "r"(1));
         *sfail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -335,10 +334,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             const int nd = dhi - dlo, units = nd + (phi - plo);
             if (builder) {
                 const int btid = tid;
-                if (bulk) tc_prefetch_bulk(a, zb0, &zbar[0], soff, runs, 0, btid);
-                else tc_prefetch(a, zb0, soff, 0, btid);
+                if (!bulk) tc_prefetch(a, zbuf(0), soff, 0, btid);
                 for (int ch = 0; ch < nchunks; ++ch) {
-                    const int s = ch & 1;
+                    const int s = ch & 1, zi = ch & (kTcZBuf - 1);
                     unsigned char* stage = sm + a.off_stage + s * kTcStageBytes;
                     unsigned char* msk = stage + 4 * 8192;
                     // thread 0 waits until the MMAs that last read this stage are done and
@@ -350,22 +348,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                         pend &= ~(1u << s);
                     }
                     if (bulk) {
-                        if (btid == 0 && !tc_wait(&zbar[s], (ph_z >> s) & 1u)) atomicExch(sfail, 1);
-                        ph_z ^= 1u << s;
+                        if (btid == 0 && !tc_wait(&zbar[zi], (ph_z >> zi) & 1u)) atomicExch(sfail, 1);
+                        ph_z ^= 1u << zi;
                     } else {
                         asm volatile("cp.async.wait_group 0;" ::: "memory");
                     }
                     asm volatile("bar.sync 1, %0;" ::"n"(kTcBuilders) : "memory");
                     if (*(volatile int*)sfail) break;
-                    if (ch + 1 < nchunks) {
-                        if (bulk) tc_prefetch_bulk(a, (ch & 1) ? zb0 : zb1, &zbar[(ch + 1) & 1], soff, runs, ch + 1, btid);
-                        else tc_prefetch(a, (ch & 1) ? zb0 : zb1, soff, ch + 1, btid);
-                    }
-                    const cfloat* zs = (ch & 1) ? zb1 : zb0;
-                    // one striped work list so that every builder does about the same:
-                    // KR items (unit = diagonal i or pair o) x 4 samples, then mask items
-                    // (pixel row x 16 samples)
-                    const int nkr = 8 * units;
+                    if (!bulk && ch + 1 < nchunks) tc_prefetch(a, zbuf(ch + 1), soff, ch + 1, btid);
+                    const cfloat* zs = zbuf(ch);
+                    // one striped work list: KR items (component x 8 samples; consecutive
+                    // lanes take consecutive components, i.e. consecutive operand rows),
+                    // then mask items (pixel row x 16 samples)
+                    const int comps = e1 - e0, nkr = 4 * comps;
                     for (int t = btid; t < nkr + 2 * kTcN; t += kTcBuilders) {
                         if (t >= nkr) {
                             const int m = t - nkr, row = m >> 1, half = m & 1;
@@ -374,48 +369,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                             *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(b >> 8);
                             continue;
                         }
-                        int g = 0, u = t;  // g = t / units (g < 8) without a division
-#pragma unroll
-                        for (int q = 0; q < 3; ++q) {
-                            const int step = units << (2 - q);
-                            if (u >= step) {
-                                u -= step;
-                                g += 4 >> q;
-                            }
-                        }
-                        const int kb = 4 * g;
+                        const int g = (t >= comps) + (t >= 2 * comps) + (t >= 3 * comps), u = t - g * comps;
+                        const int kb = 8 * g, e = e0 + u;
                         const cfloat* zk = zs + kb * n;  // sample kb; + n per sample
-                        if (u < nd) {
-                            const int i = dlo + u, e = i - e0;
-                            float x[4];
-                            const cfloat* zi = zk + i;
+                        float x[8];
+                        if (e < n) {
+                            const cfloat* pi = zk + e;
 #pragma unroll
-                            for (int q = 0; q < 4; ++q, zi += n) x[q] = cabs2(*zi);
-                            unsigned char* hp = stage + (e >> 7) * 16384;
-                            tc_store4(hp, hp + 8192, e & 127, kb, x);
+                            for (int q = 0; q < 8; ++q, pi += n) x[q] = cabs2(*pi);
                         } else {
-                            const int o = plo + u - nd;
-                            const uint32_t ij = pairs[o];
-                            const int i = ij & 0xffff, j = ij >> 16;
-                            float re[4], im[4];
-                            const cfloat* pi = zk + i;
-                            const cfloat* pj = zk + j;
+                            const uint32_t ij = pairs[(e - n) >> 1];
+                            const bool imag = (e - n) & 1;
+                            const cfloat* pi = zk + (ij & 0xffff);
+                            const cfloat* pj = zk + (ij >> 16);
 #pragma unroll
-                            for (int q = 0; q < 4; ++q, pi += n, pj += n) {
+                            for (int q = 0; q < 8; ++q, pi += n, pj += n) {
                                 const cfloat zi = *pi, zj = *pj;
-                                re[q] = fmaf(zi.re, zj.re, zi.im * zj.im);    // Re z_i conj(z_j)
-                                im[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
-                            }
-                            const int er = n + 2 * o;
-                            if (er >= e0 && er < e1) {
-                                unsigned char* hp = stage + ((er - e0) >> 7) * 16384;
-                                tc_store4(hp, hp + 8192, (er - e0) & 127, kb, re);
-                            }
-                            if (er + 1 >= e0 && er + 1 < e1) {
-                                unsigned char* hp = stage + ((er + 1 - e0) >> 7) * 16384;
-                                tc_store4(hp, hp + 8192, (er + 1 - e0) & 127, kb, im);
+                                const float re = fmaf(zi.re, zj.re, zi.im * zj.im);    // Re z_i conj(z_j)
+                                const float im = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
+                                x[q] = imag ? im : re;
                             }
                         }
+                        unsigned char* hp = stage + (u >> 7) * 16384;
+                        tc_store8(hp, hp + 8192, u & 127, kb, x);
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
@@ -437,6 +413,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 // MMA issuer
                 constexpr uint32_t LBO = 128, SBO = kTcKC / 8 * 128;
                 const uint32_t idesc = tc_idesc_bf16(kTcM, kTcN);
+                if (bulk)
+                    for (int c = 0; c < kTcZBuf && c < nchunks; ++c) tc_prefetch_bulk(a, zbuf(c), &zbar[c], runs, c);
                 for (int ch = 0; ch < nchunks; ++ch) {
                     const int s = ch & 1;
                     if (!tc_wait(&full[s], (ph_full >> s) & 1u)) {
@@ -469,6 +447,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                      tc_smem(&empty[s]))
                                  : "memory");
+                    // the builders are done with this chunk's samples: refill its buffer
+                    if (bulk && ch + kTcZBuf < nchunks)
+                        tc_prefetch_bulk(a, zbuf(ch), &zbar[ch & (kTcZBuf - 1)], runs, ch + kTcZBuf);
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -570,7 +570,7 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
     };
     a.off_stage = take(2 * (size_t)kTcStageBytes, 1024);
     a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
-    a.off_z = take(2 * (size_t)a.z_bytes, 16);
+    a.off_z = take(kTcZBuf * (size_t)a.z_bytes, 16);
     a.off_r = take((size_t)kTcN * a.ld_r * sizeof(float), 16);
     a.off_pbits = take((size_t)kTcN * a.kwords * sizeof(uint32_t), 16);
     a.off_soff = take((size_t)a.kpad * sizeof(int), 16);
