@@ -38,6 +38,10 @@ ALPHA = 0.001
 PS_THR = 0.25
 SEED = 20261205
 METRIC = "phase-linked pixels/sec (N=30, EMI) chosen vs plain GPU form at <=1e-3 rad; GB/s"
+# DRAM bytes (read + write) of one k_cov_tc launch on a 1034x1046-pixel block of this
+# workload, from an ncu capture (dram__bytes_read.sum 578,324,736 + dram__bytes_write.sum
+# 3,748,861,696); the planar coherence output (N^2 floats per pixel) is most of it
+COV_TC_TRAFFIC = 578_324_736 + 3_748_861_696
 UNIT = "pixels/s"
 
 
@@ -192,7 +196,7 @@ def max_over_ranks(values, dist, device=None):
     return vals.tolist()
 
 
-def gpu_step(stack, plan, dp, outputs):
+def gpu_step(stack, plan, dp, outputs, covariance_form="tensor", use_evd=False):
     """One pass of the hot path over every block of a device-resident stack."""
     cpx_full, tc_full = outputs
     for (ir, ic, tr, tcl, orr, occ) in plan:
@@ -200,9 +204,24 @@ def gpu_step(stack, plan, dp, outputs):
         mean, disp, ps = dp.calc_ps_block(blk.abs(), PS_THR, NSLC)
         var = (disp * mean) ** 2
         nb = dp.estimate_neighbors(halfwin_rowcol=HALF, alpha=ALPHA, mean=mean, var=var, nslc=NSLC)
-        out = dp.run_phase_linking(blk, HALF, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, compute_crlb=True)
+        out = dp.run_phase_linking(blk, HALF, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, compute_crlb=True,
+                                   use_evd=use_evd, covariance_form=covariance_form)
         cpx_full[:, orr[0]:orr[1], occ[0]:occ[1]] = out.cpx_phase[:, tr[0]:tr[1], tcl[0]:tcl[1]]
         tc_full[orr[0]:orr[1], occ[0]:occ[1]] = out.temp_coh[tr[0]:tr[1], tcl[0]:tcl[1]]
+
+
+def form_rate(torch, stack, plan, dp, outputs, **kw):
+    """Output pixels/s of one timed pass over `plan` (after one untimed pass)."""
+    gpu_step(stack, plan, dp, outputs, **kw)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    gpu_step(stack, plan, dp, outputs, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    px = sum((orr[1] - orr[0]) * (occ[1] - occ[0]) for (*_x, orr, occ) in plan)
+    return px / (e0.elapsed_time(e1) / 1000.0)
 
 
 def run_ours(args, rank, world, pool, cores):
@@ -261,6 +280,13 @@ def run_ours(args, rank, world, pool, cores):
     cov_ms = tot[0] / max(cnt[0], 1)   # per launch (one launch per block)
     sol_ms = tot[1] / max(cnt[1], 1)
     launches_cov = cnt[0] / args.steps
+
+    # ---- the same stack through the plain GPU form (SIMT covariance fused with the
+    # solver) and through EVD, on the first two blocks ----
+    sub = plan[:2]
+    plain_rate = form_rate(torch, stack, sub, dp, (cpx_full, tc_full), covariance_form="simt")
+    chosen_rate = form_rate(torch, stack, sub, dp, (cpx_full, tc_full))
+    evd_rate = form_rate(torch, stack, sub, dp, (cpx_full, tc_full), use_evd=True)
 
     # ---- end-to-end: pinned host stack in, host results out, through the public API ----
     host_stack = torch.empty(stack.shape, dtype=stack.dtype, pin_memory=True)
@@ -342,7 +368,7 @@ def run_ours(args, rank, world, pool, cores):
         "e2e": {"value": px / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_per_step * args.steps),
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": COV_TC_TRAFFIC if frame == FRAME else None,
                      "kernel": "k_cov_tc", "kernel_ms": cov_ms, "launches_per_step": launches_cov,
                      "note": "algorithmic covariance flops 4*W*N*(N+1) per pixel over the measured launch time "
                              "(CUDA events on the launch stream); peak = measured bf16 dense (of measured)"},
@@ -352,6 +378,10 @@ def run_ours(args, rank, world, pool, cores):
                    "note": "FP32 CUDA-core bound; algorithmic flops ~(3N^3 + 56N^2) per pixel; nominal peak, "
                            "no measured FP32 figure"},
         "clocks": clocks,
+        "forms": {"blocks": len(sub), "unit": UNIT, "chosen": chosen_rate, "plain": plain_rate,
+                  "chosen_over_plain": chosen_rate / plain_rate, "evd_chosen": evd_rate,
+                  "note": "chosen = tensor-core covariance + register solver; plain = SIMT covariance fused "
+                          "with the shared-memory solver; both EMI unless evd"},
     }
     if cpu:
         line["cpu_baseline"] = cpu
