@@ -5,6 +5,7 @@ Public entry points keep the reference's names, arguments and outputs:
 * :func:`run_phase_linking`  (dolphin.phase_link.run_phase_linking)
 * :func:`estimate_neighbors` (dolphin.shp.estimate_neighbors)
 * :func:`calc_ps_block`      (dolphin.ps.calc_ps_block)
+* :func:`compress`           (dolphin.phase_link.compress)
 
 All compute runs in hand-written CUDA kernels for sm_103a behind the C ABI in
 ``include/dpl.h`` (``dolphin_gb300/_lib/libdpl.so``).  Importing this package
@@ -14,6 +15,7 @@ does not initialise CUDA, so it is safe in spawned worker processes.
 from __future__ import annotations
 
 from ._types import HalfWindow, ShpMethod, Strides
+from .compress import compress
 from .phase_link import (
     EstimatorType,
     PhaseLinkOutput,
@@ -33,6 +35,7 @@ __all__ = [
     "ShpMethod",
     "Strides",
     "calc_ps_block",
+    "compress",
     "estimate_neighbors",
     "estimate_stack_covariance",
     "install_into_dolphin",
@@ -49,6 +52,9 @@ _PATCH_TARGETS = (
     ("dolphin.shp", "estimate_neighbors"),
     ("dolphin.ps", "calc_ps_block"),
     ("dolphin.workflows.single", "calc_ps_block"),
+    ("dolphin.phase_link", "compress"),
+    ("dolphin.phase_link._compress", "compress"),
+    ("dolphin.workflows.single", "compress"),
 )
 
 
@@ -69,6 +75,7 @@ def install_into_dolphin(modules=None):
         "run_phase_linking": run_phase_linking,
         "estimate_neighbors": estimate_neighbors,
         "calc_ps_block": calc_ps_block,
+        "compress": compress,
     }
     patched = []
 

@@ -66,6 +66,7 @@ SIGNATURES = {
     "dpl_covariance": (_i, [_p, _i64, _i64, _i64, _i, _i, _i, _i, _p, _i, _p, _p, _sz, _p]),
     "dpl_process_coherence_workspace_size": (_sz, [_i64]),
     "dpl_process_coherence": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _sz, _p]),
+    "dpl_compress": (_i, [_p, _i64, _i64, _i64, _p, _i64, _i64, _i, _p, _i, _i, _p, _p]),
     "dpl_process_coherence_noalloc_max_pixels": (_i64, []),
     "dpl_process_coherence_noalloc": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p]),
     "dpl_kernel_timing": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

@@ -168,6 +168,21 @@ dpl_status dpl_process_coherence(const float* C, int64_t npix, int nslc, int use
                                  float* crlb_std_dev, float* temp_coh, float* closure_phases,
                                  void* workspace, size_t workspace_bytes, dpl_stream_t stream);
 
+/* Replaces: _compress.compress(slc_stack, pl_cpx_phase, first_real_slc_idx, slc_mean,
+ *           reference_idx) -- phase_link/_compress.py:11-65 (with utils.upsample_nearest,
+ *           utils.py:281-324).
+ * slc          : (nslc, rows, cols) complex64
+ * pl_cpx_phase : (nslc, pl_rows, pl_cols) complex64, upsampled by block repetition
+ *                (rows / pl_rows, cols / pl_cols), zero beyond the repeats
+ * slc_mean     : (rows, cols) float32 in/out or NULL (then mean |z| over the real SLCs);
+ *                set to NaN where the projected phase is exactly 0, as the reference does
+ * has_reference: re-reference pl_cpx_phase to reference_idx (0 <= idx < nslc) first
+ * comp_slc     : (rows, cols) complex64 out */
+dpl_status dpl_compress(const float* slc, int64_t nslc, int64_t rows, int64_t cols,
+                        const float* pl_cpx_phase, int64_t pl_rows, int64_t pl_cols,
+                        int first_real_slc_idx, float* slc_mean, int has_reference,
+                        int reference_idx, float* comp_slc, dpl_stream_t stream);
+
 /* No counterpart in the reference: dpl_process_coherence without a caller-supplied
  * workspace, for callers that cannot allocate device memory per call (a C/GDAL-style
  * host that owns no device allocator and cannot size one, or a multi-stream pipeline

@@ -30,6 +30,7 @@ __all__ = [
     "PhaseLinkRuntimeError",
     "calc_ps_block",
     "closure_phases",
+    "compress",
     "compute_out_shape",
     "decimate",
     "estimate_neighbors",
@@ -45,6 +46,7 @@ __all__ = [
     "process_coherence_matrices",
     "run_phase_linking",
     "take_looks",
+    "upsample_nearest",
 ]
 
 
@@ -799,3 +801,43 @@ def run_phase_linking(slc_stack, half_window, strides=(1, 1), use_evd=False, bet
         crlb_std_dev=np.array(cpl.crlb_std_dev),
         closure_phases=np.asarray(cpl.closure_phases),
     )
+
+
+# --------------------------------------------------------------------------------------
+# compressed SLC (phase_link/_compress.py:11-65)
+# --------------------------------------------------------------------------------------
+def upsample_nearest(arr, output_shape, looks=None):
+    """Block repetition to `output_shape`, zero where the repeats do not reach (utils.py:281-324)."""
+    in_rows, in_cols = arr.shape[-2:]
+    out_rows, out_cols = output_shape[-2:]
+    if (in_rows, in_cols) == (out_rows, out_cols):
+        return arr
+    ry, rx = (out_rows // in_rows, out_cols // in_cols) if looks is None else looks
+    up = np.repeat(np.repeat(arr, ry, axis=-2), rx, axis=-1)
+    r, c = min(out_rows, up.shape[-2]), min(out_cols, up.shape[-1])
+    out = np.zeros(arr.shape[:-2] + (out_rows, out_cols), dtype=arr.dtype)
+    out[..., :r, :c] = up[..., :r, :c]
+    return out
+
+
+def compress(slc_stack, pl_cpx_phase, first_real_slc_idx=0, slc_mean=None, reference_idx=None):
+    """Compressed SLC: mean amplitude x phase of sum_t z_t conj(pl_t) (phase_link/_compress.py:11-65).
+
+    The phase-linked phases are re-referenced to `reference_idx` (if given) before the
+    compressed layers (index < first_real_slc_idx) are dropped; NaN products are
+    skipped (nansum); where that phase is exactly 0 the magnitude becomes NaN, and a
+    given `slc_mean` is modified in place accordingly, as in the reference.
+    """
+    pl = np.asarray(pl_cpx_phase)
+    if reference_idx is not None:
+        pl = pl * pl[reference_idx][None, :, :].conj()
+    pl = pl[first_real_slc_idx:]
+    slcs = np.asarray(slc_stack)[first_real_slc_idx:]
+    pl_up = upsample_nearest(pl, slcs.shape[1:])
+    with warnings.catch_warnings():
+        warnings.filterwarnings("ignore", message="invalid value encountered")
+        phase = np.angle(np.nansum(slcs * np.conjugate(pl_up), axis=0))
+    if slc_mean is None:
+        slc_mean = np.mean(np.abs(slcs), axis=0)
+    slc_mean[phase == 0] = np.nan
+    return slc_mean * np.exp(1j * phase)

@@ -246,9 +246,40 @@ def make_ps_fill():
     _save("ps_fill", **out)
 
 
+def make_compress():
+    """compress() on seeded stacks: strides 1 and 3, referencing, compressed layers, NaNs."""
+    out = {}
+    cases = [
+        # (seed, n, rows, cols, strides, first_real, ref, with_mean)
+        (701, 10, 11, 11, (1, 1), 0, -1, False),
+        (702, 10, 11, 11, (3, 3), 0, -1, False),
+        (703, 14, 12, 17, (2, 3), 2, 1, True),
+        (704, 8, 9, 10, (1, 1), 0, 3, True),
+    ]
+    for k, (seed, n, rows, cols, st, first, ref, with_mean) in enumerate(cases):
+        rng = np.random.default_rng(seed)
+        z = make_stack(StackConfig(nslc=n, rows=rows, cols=cols, seed=seed, ps_frac=0.0))
+        z[1, 2, 3] = np.nan + 1j * np.nan  # one NaN sample
+        z[:, 4, 5] = np.nan  # a pixel with no valid sample
+        orow, ocol = rows // st[0], cols // st[1]
+        ph = rng.uniform(-np.pi, np.pi, size=(n, orow, ocol))
+        pl = np.exp(1j * ph).astype(np.complex64)
+        pl[:, 0, 0] = np.nan  # a NaN phase-linked pixel
+        mean = (np.abs(z[first:]).mean(axis=0) * 1.5).astype(np.float32) if with_mean else None
+        mean_in = None if mean is None else mean.copy()
+        comp = R.compress.compress(z.copy(), pl.copy(), first_real_slc_idx=first,
+                                   slc_mean=mean, reference_idx=None if ref < 0 else ref)
+        out[f"slc_{k}"], out[f"pl_{k}"], out[f"out_{k}"] = z, pl, np.asarray(comp)
+        out[f"params_{k}"] = np.array([first, ref, int(with_mean)])
+        if with_mean:
+            out[f"mean_in_{k}"], out[f"mean_after_{k}"] = mean_in, mean
+    _save("compress", ncases=np.array(len(cases)), **out)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["ps", "glrt", "ks", "covariance", "phase_link", "config1", "ps_fill"]
+    which = sys.argv[1:] or ["ps", "glrt", "ks", "covariance", "phase_link", "config1", "ps_fill", "compress"]
     for w in which:
         print(f"[{w}]")
         {"ps": make_ps, "glrt": make_glrt, "ks": make_ks, "covariance": make_covariance,
-         "phase_link": make_phase_link, "config1": make_config1_crop, "ps_fill": make_ps_fill}[w]()
+         "phase_link": make_phase_link, "config1": make_config1_crop, "ps_fill": make_ps_fill,
+         "compress": make_compress}[w]()

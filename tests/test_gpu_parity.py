@@ -426,3 +426,52 @@ def test_config2_crop_tensor_vs_float64():
     assert err.max() < PHASE_TOL, err.max()
     assert np.abs(out.temp_coh[good] - ref64.temp_coh[good]).max() < TC_TOL
     np.testing.assert_array_equal(out.estimator[~border], ref64.estimator[~border])
+
+
+# ---------------------------------------------------------------------------------
+# compressed SLC (phase_link/_compress.py:11-65)
+# ---------------------------------------------------------------------------------
+def test_compress_golden(golden):
+    g = golden("compress")
+    for k in range(int(g["ncases"])):
+        first, ref, with_mean = (int(x) for x in g[f"params_{k}"])
+        mean = g[f"mean_in_{k}"].copy() if with_mean else None
+        out = dp.compress(g[f"slc_{k}"], g[f"pl_{k}"], first_real_slc_idx=first, slc_mean=mean,
+                          reference_idx=None if ref < 0 else ref)
+        want = g[f"out_{k}"]
+        assert out.dtype == np.complex64 and out.shape == want.shape
+        np.testing.assert_array_equal(np.isnan(out), np.isnan(want))
+        ok = ~np.isnan(want)
+        np.testing.assert_allclose(np.abs(out[ok]), np.abs(want[ok]), rtol=2e-6)
+        assert phase_err(out[ok], want[ok]).max() < 1e-5
+        if with_mean:
+            np.testing.assert_array_equal(np.isnan(mean), np.isnan(g[f"mean_after_{k}"]))
+
+
+@pytest.mark.parametrize("strides", [1, 3])
+def test_compress_magnitude_is_stack_mean(strides):
+    # the reference's own property test (tests/test_phase_link_compress.py): with the
+    # stack's phase-linked phase, |compressed| is the mean amplitude, NaN beyond the
+    # upsampled area
+    z = make_stack(StackConfig(nslc=10, rows=11, cols=11, seed=77, ps_frac=0.0))
+    out = dp.run_phase_linking(z, (3, 3), (strides, strides), compute_crlb=False)
+    comp = dp.compress(z, out.cpx_phase)
+    vr, vc = 11 // strides * strides, 11 // strides * strides
+    np.testing.assert_allclose(np.abs(comp)[:vr, :vc], np.abs(z).mean(axis=0)[:vr, :vc], rtol=1e-5)
+    assert np.isnan(np.abs(comp)[vr:, :]).all() and np.isnan(np.abs(comp)[:, vc:]).all()
+    rc = O.compress(z, out.cpx_phase)
+    assert phase_err(comp[:vr, :vc], rc[:vr, :vc]).max() < 1e-5
+
+
+def test_compress_device_tensors_and_errors():
+    z = make_stack(StackConfig(nslc=6, rows=8, cols=9, seed=78, ps_frac=0.0))
+    pl = np.exp(1j * np.angle(z)).astype(np.complex64)
+    mean = torch.from_numpy(np.abs(z).mean(axis=0).astype(np.float32)).cuda()
+    comp = dp.compress(torch.from_numpy(z).cuda(), torch.from_numpy(pl).cuda(), slc_mean=mean, reference_idx=-1)
+    assert comp.is_cuda and comp.dtype == torch.complex64
+    rc = O.compress(z, pl, slc_mean=np.abs(z).mean(axis=0).astype(np.float32), reference_idx=5)
+    assert phase_err(comp.cpu().numpy(), rc).max() < 1e-5
+    with pytest.raises(IndexError):
+        dp.compress(z, pl, reference_idx=6)
+    with pytest.raises(ValueError):
+        dp.compress(z, pl[:3])

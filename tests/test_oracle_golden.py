@@ -113,3 +113,16 @@ def test_all_nan_slc_raises():
     z[1] = np.nan
     with pytest.raises(O.PhaseLinkRuntimeError, match="are all NaNs"):
         O.run_phase_linking(z, (1, 1))
+
+
+def test_compress_matches_reference(golden):
+    g = golden("compress")
+    for k in range(int(g["ncases"])):
+        first, ref, with_mean = (int(x) for x in g[f"params_{k}"])
+        mean = g[f"mean_in_{k}"].copy() if with_mean else None
+        out = O.compress(g[f"slc_{k}"], g[f"pl_{k}"], first_real_slc_idx=first, slc_mean=mean,
+                         reference_idx=None if ref < 0 else ref)
+        np.testing.assert_array_equal(np.isnan(out), np.isnan(g[f"out_{k}"]))
+        np.testing.assert_allclose(out, g[f"out_{k}"], rtol=1e-6, atol=1e-6, equal_nan=True)
+        if with_mean:  # the given mean is modified in place, as the reference does
+            np.testing.assert_array_equal(np.isnan(mean), np.isnan(g[f"mean_after_{k}"]))
