@@ -388,6 +388,44 @@ def run_ours(args, rank, world, pool, cores):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args):
+    """Rates of the two covariance forms on the precision workload (one GPU)."""
+    import torch
+
+    import dolphin_gb300 as dp
+    from dolphin_gb300._build import build_library
+    from dolphin_gb300.simulate import StackConfig, make_stack_torch
+
+    build_library()
+    n, frame, half = 40, 2048, (7, 7)
+    cfg = StackConfig(nslc=n, rows=frame, cols=frame, seed=20261206, gamma_inf=0.02, disk_gamma0=0.95,
+                      disk_radius=0.125, ps_frac=0.0)
+    stack = make_stack_torch(cfg)
+    plan = block_plan(frame, frame, BLOCK, half)
+    rates = {}
+    for form in ("tensor", "simt"):
+        def step():
+            for (ir, ic, *_r) in plan:
+                blk = stack[:, ir[0]:ir[1], ic[0]:ic[1]].contiguous()
+                mean, disp, _ps = dp.calc_ps_block(blk.abs(), PS_THR, n)
+                nb = dp.estimate_neighbors(halfwin_rowcol=half, alpha=ALPHA, mean=mean, var=(disp * mean) ** 2,
+                                           nslc=n)
+                dp.run_phase_linking(blk, half, neighbor_arrays=nb, covariance_form=form)
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(max(1, args.steps)):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        rates[form] = frame * frame * max(1, args.steps) / (e0.elapsed_time(e1) / 1000.0)
+    print(json.dumps({"workload": "precision", "config": {"nslc": n, "frame": frame, "half_window": half,
+                                                          "gamma_inf": 0.02, "disk_gamma0": 0.95},
+                      "unit": UNIT, "rates": rates, "tensor_over_simt": rates["tensor"] / rates["simt"]}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -396,11 +434,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frame", type=int, default=FRAME)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--workload", default="config2", choices=["config2", "precision"],
+                    help="precision: N=40 2048x2048 stack, half-window (7, 7), low gamma_inf with a "
+                         "high-coherence disk; rates of the tensor-core and SIMT covariance forms")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "precision":
+        run_precision(args)
         return
     pool = None
     cores = len(os.sched_getaffinity(0))

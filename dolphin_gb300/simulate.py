@@ -45,6 +45,10 @@ class StackConfig:
     ps_amp: float = 10.0
     ps_amp_jitter: float = 0.01
     ps_phase_std: float = 0.05
+    # optional high-coherence disk (centred, radius disk_radius * max(rows, cols)) whose
+    # pixels follow the model with gamma0 = disk_gamma0 instead
+    disk_gamma0: float | None = None
+    disk_radius: float = 0.125
 
 
 def coherence_model(nslc, gamma0, gamma_inf, tau, acq_interval=12.0):
@@ -54,6 +58,14 @@ def coherence_model(nslc, gamma0, gamma_inf, tau, acq_interval=12.0):
     g = (gamma0 - gamma_inf) * np.exp(-dt / tau) + gamma_inf
     np.fill_diagonal(g, 1.0)
     return g
+
+
+def _disk_mask(cfg, r0=0, r1=None):
+    rows, cols = cfg.rows, cfg.cols
+    r1 = rows if r1 is None else r1
+    r = np.arange(r0, r1)[:, None] - rows / 2.0
+    c = np.arange(cols)[None, :] - cols / 2.0
+    return r * r + c * c <= (cfg.disk_radius * max(rows, cols)) ** 2
 
 
 def _defo_phase(nslc, rows, cols, peak):
@@ -76,6 +88,10 @@ def make_stack(cfg: StackConfig = StackConfig(), return_truth=False):
     w = (rng.normal(scale=np.sqrt(0.5), size=(n, npx))
          + 1j * rng.normal(scale=np.sqrt(0.5), size=(n, npx)))
     x = (L @ w).reshape(n, rows, cols)
+    if cfg.disk_gamma0 is not None:
+        Ld = np.linalg.cholesky(coherence_model(n, cfg.disk_gamma0, cfg.gamma_inf, cfg.tau, cfg.acq_interval))
+        disk = _disk_mask(cfg)
+        x[:, disk] = (Ld @ w)[:, disk.ravel()]
     amp = rng.lognormal(mean=0.0, sigma=cfg.amp_sigma, size=(n, rows, cols))
     phi = _defo_phase(n, rows, cols, cfg.defo_peak)
     z = amp * np.exp(1j * phi) * x
@@ -105,6 +121,10 @@ def make_stack_torch(cfg: StackConfig, device="cuda", rows_chunk=1024):
     gamma = coherence_model(n, cfg.gamma0, cfg.gamma_inf, cfg.tau, cfg.acq_interval)
     L = torch.tensor(np.linalg.cholesky(gamma), dtype=torch.float32, device=device)
     Lc = torch.complex(L, torch.zeros_like(L))
+    if cfg.disk_gamma0 is not None:
+        Ld = torch.tensor(np.linalg.cholesky(coherence_model(n, cfg.disk_gamma0, cfg.gamma_inf, cfg.tau,
+                                                             cfg.acq_interval)), dtype=torch.float32, device=device)
+        Ldc = torch.complex(Ld, torch.zeros_like(Ld))
     out = torch.empty((n, rows, cols), dtype=torch.complex64, device=device)
     phi_full = torch.tensor(_defo_phase(n, rows, cols, cfg.defo_peak), dtype=torch.float32, device=device)
     for r0 in range(0, rows, rows_chunk):
@@ -115,6 +135,10 @@ def make_stack_torch(cfg: StackConfig, device="cuda", rows_chunk=1024):
             torch.randn((n, npx), generator=g, device=device) * np.sqrt(0.5),
         )
         x = (Lc @ w).reshape(n, r1 - r0, cols)
+        if cfg.disk_gamma0 is not None:
+            disk = torch.tensor(_disk_mask(cfg, r0, r1), device=device)
+            xd = (Ldc @ w).reshape(n, r1 - r0, cols)
+            x = torch.where(disk[None], xd, x)
         amp = torch.exp(cfg.amp_sigma * torch.randn((n, r1 - r0, cols), generator=g, device=device))
         phi = phi_full[:, r0:r1]
         z = amp * torch.polar(torch.ones_like(phi), phi) * x

@@ -1,0 +1,57 @@
+"""Precision form: N=40, half-window (7, 7), gamma_inf 0.02 with a high-coherence disk
+(gamma0 0.95), GLRT SHPs, EMI.  Each covariance form's phase and temporal-coherence error
+against the float64 oracle, on a crop that holds both the disk and its surroundings.
+
+Run with ``-s`` to see the per-form error table.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import phase_link as O
+from parity import phase_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover - CPU container
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import dolphin_gb300 as dp  # noqa: E402
+from dolphin_gb300.simulate import StackConfig, make_stack  # noqa: E402
+
+HW = (7, 7)
+CFG = StackConfig(nslc=40, rows=72 + 14, cols=72 + 14, seed=20261206, gamma_inf=0.02, disk_gamma0=0.95,
+                  disk_radius=0.3, ps_frac=0.0)
+
+
+@pytest.fixture(scope="module")
+def case():
+    z = make_stack(CFG)
+    mean, disp, _ps = dp.calc_ps_block(np.abs(z), 0.25, CFG.nslc)
+    nb = dp.estimate_neighbors(halfwin_rowcol=HW, alpha=0.001, mean=mean, var=(disp * mean) ** 2, nslc=CFG.nslc)
+    diag = {}
+    ref = O.run_phase_linking(z, HW, neighbor_arrays=nb, dtype=np.float64, diagnostics=diag)
+    r = np.arange(CFG.rows)[:, None] - CFG.rows / 2.0
+    c = np.arange(CFG.cols)[None, :] - CFG.cols / 2.0
+    disk = r * r + c * c <= (CFG.disk_radius * max(CFG.rows, CFG.cols)) ** 2
+    return z, nb, ref, diag, disk
+
+
+@pytest.mark.parametrize("form", ["tensor", "simt"])
+def test_precision_form_vs_float64(case, form):
+    z, nb, ref, diag, disk = case
+    out = dp.run_phase_linking(z, HW, neighbor_arrays=nb, covariance_form=form)
+    border = diag["gamma_min_eig"] < 1e-3
+    good = (ref.temp_coh > 0.3) & ~border & np.all(np.isfinite(ref.cpx_phase), axis=0)
+    assert good.mean() > 0.5
+    rows = []
+    for name, sel in (("disk", good & disk), ("outside", good & ~disk), ("all", good)):
+        err = phase_err(out.cpx_phase[:, sel], ref.cpx_phase[:, sel].astype(np.complex64))
+        tce = np.abs(out.temp_coh[sel] - ref.temp_coh[sel])
+        rows.append((name, int(sel.sum()), err.max(), np.percentile(err, 99), tce.max()))
+    for name, npx, emax, e99, tmax in rows:
+        print(f"[precision] form={form:6s} {name:8s} pixels={npx:5d} phase err max {emax:.2e} "
+              f"p99 {e99:.2e} rad, temp_coh err max {tmax:.2e}")
+    assert rows[-1][2] < 1e-3
+    assert rows[-1][4] < 1e-4
