@@ -426,6 +426,61 @@ def run_precision(args):
           flush=True)
 
 
+BATCH_DEPTHS = (8, 10, 12, 15, 18, 20, 24, 28, 32, 36, 40, 45)
+
+
+def run_batch(args):
+    """Ministack batch: PS + GLRT + phase linking of 12 stacks of uneven depth, eager and
+    as one CUDA-graph replay, with the per-depth covariance form picked by tune_forms."""
+    import torch
+
+    from dolphin_gb300 import PhaseLinkBatch, tune_forms
+    from dolphin_gb300._build import build_library
+    from dolphin_gb300.simulate import StackConfig, make_stack_torch
+
+    build_library()
+    side, half, seed = 1024, (5, 5), 20261207
+    rng = np.random.default_rng(seed)
+    taus = rng.uniform(24.0, 96.0, size=len(BATCH_DEPTHS))
+    stacks = [make_stack_torch(StackConfig(nslc=n, rows=side, cols=side, seed=seed + k, tau=float(taus[k]),
+                                           ps_frac=0.03, outlier_frac=0.4))
+              for k, n in enumerate(BATCH_DEPTHS)]
+    forms = tune_forms(BATCH_DEPTHS, half)
+    px = len(stacks) * side * side
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    reps = max(1, args.steps)
+    eager = PhaseLinkBatch(stacks, half, forms=forms, graph=False)
+    eager_ms = timed(eager.run, reps)
+    graph = PhaseLinkBatch(stacks, half, forms=forms, graph=True)
+    graph_ms = timed(graph.run, reps)
+    # per-ministack latency (eager, one stack per call)
+    lat = []
+    for _ in range(reps):
+        for z in stacks:
+            one = PhaseLinkBatch([z], half, forms=forms, graph=False)
+            lat.append(timed(one.run, 1))
+    print(json.dumps({
+        "workload": "batch", "unit": UNIT,
+        "config": {"depths": list(BATCH_DEPTHS), "side": side, "half_window": half, "tau_days": taus.round(1).tolist(),
+                   "outlier_frac": 0.4, "ps_frac": 0.03},
+        "forms": {str(k): v for k, v in forms.items()},
+        "eager": px / (eager_ms / 1000.0), "graph": px / (graph_ms / 1000.0),
+        "ms_per_batch": {"eager": eager_ms, "graph": graph_ms},
+        "ministack_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -434,9 +489,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frame", type=int, default=FRAME)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--workload", default="config2", choices=["config2", "precision"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "precision", "batch"],
                     help="precision: N=40 2048x2048 stack, half-window (7, 7), low gamma_inf with a "
-                         "high-coherence disk; rates of the tensor-core and SIMT covariance forms")
+                         "high-coherence disk; rates of the tensor-core and SIMT covariance forms. "
+                         "batch: 12 ministacks of N = 8..45, 1024x1024 each, as one CUDA graph")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -445,6 +501,9 @@ def main():
         return
     if args.workload == "precision":
         run_precision(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
         return
     pool = None
     cores = len(os.sched_getaffinity(0))

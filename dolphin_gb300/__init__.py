@@ -15,6 +15,7 @@ does not initialise CUDA, so it is safe in spawned worker processes.
 from __future__ import annotations
 
 from ._types import HalfWindow, ShpMethod, Strides
+from .batch import PhaseLinkBatch, tune_forms
 from .compress import compress
 from .phase_link import (
     EstimatorType,
@@ -30,6 +31,7 @@ from .shp import estimate_neighbors
 __all__ = [
     "EstimatorType",
     "HalfWindow",
+    "PhaseLinkBatch",
     "PhaseLinkOutput",
     "PhaseLinkRuntimeError",
     "ShpMethod",
@@ -41,6 +43,7 @@ __all__ = [
     "install_into_dolphin",
     "process_coherence_matrices",
     "run_phase_linking",
+    "tune_forms",
 ]
 
 # (module, attribute) pairs of an installed dolphin that bind the hot path by name

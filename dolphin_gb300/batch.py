@@ -1,0 +1,175 @@
+"""Ministack batches: several phase-linking problems as one CUDA-graph replay.
+
+A sequential dolphin run processes ministacks of different depth N (e.g. 15 new SLCs
+plus the compressed SLCs of earlier ministacks).  ``PhaseLinkBatch`` takes a list of
+device-resident stacks, runs PS selection, GLRT SHP selection and phase linking for
+each, and after a first eager run captures the whole sequence once as a CUDA graph:
+later ``run()`` calls replay it with one launch, reading the (updated in place)
+input tensors and writing the same output tensors.  The per-call status (all-NaN
+SLCs, device timeouts) is checked after the replay, as ``run_phase_linking`` does.
+
+The covariance form per N (tensor cores or SIMT) is chosen by ``tune_forms``, which
+times both on a small synthetic stack of that depth once per (N, half window,
+strides) and keeps the choice in a table that can be saved and loaded as JSON.
+"""
+
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+from . import _device as D
+from . import _lib
+from .phase_link import PhaseLinkOutput, _form_code
+from .ps import calc_ps_block
+from .shp import estimate_neighbors
+
+__all__ = ["PhaseLinkBatch", "tune_forms"]
+
+_TUNED: dict[tuple, str] = {}
+
+
+def tune_forms(depths, half_window, strides=(1, 1), table_path=None, sample=96, reps=3):
+    """Pick the faster covariance form for each stack depth; returns {N: form}.
+
+    Timings use a seeded synthetic stack of ``sample x sample`` output pixels per depth.
+    ``table_path`` (JSON) is read first and written back with any new entries.
+    """
+    import torch
+
+    from .phase_link import run_phase_linking
+    from .simulate import StackConfig, make_stack_torch
+
+    hy, hx = (int(v) for v in half_window)
+    sy, sx = (int(v) for v in strides)
+    if table_path is not None and Path(table_path).exists():
+        for k, v in json.loads(Path(table_path).read_text()).items():
+            _TUNED[tuple(int(x) for x in k.split(","))] = v
+    out = {}
+    for n in sorted(set(int(d) for d in depths)):
+        key = (n, hy, hx, sy, sx)
+        if key not in _TUNED:
+            cfg = StackConfig(nslc=n, rows=sample * sy + 2 * hy, cols=sample * sx + 2 * hx, seed=1000 + n,
+                              ps_frac=0.0)
+            z = make_stack_torch(cfg)
+            best, best_ms = None, float("inf")
+            for form in ("tensor", "simt"):
+                run_phase_linking(z, (hy, hx), (sy, sx), compute_crlb=False, covariance_form=form)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    run_phase_linking(z, (hy, hx), (sy, sx), compute_crlb=False, covariance_form=form)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                if ms < best_ms:
+                    best, best_ms = form, ms
+            _TUNED[key] = best
+        out[n] = _TUNED[key]
+    if table_path is not None:
+        Path(table_path).write_text(json.dumps({",".join(map(str, k)): v for k, v in sorted(_TUNED.items())},
+                                               indent=1))
+    return out
+
+
+class PhaseLinkBatch:
+    """PS + GLRT + phase linking over a list of (N_k, rows, cols) complex64 CUDA stacks.
+
+    Parameters follow ``run_phase_linking`` (EMI/EVD, CRLB, references) and
+    ``estimate_neighbors`` (GLRT ``alpha``); ``forms`` maps N to "tensor" or "simt"
+    (default: ``tune_forms``).  ``graph=False`` runs every call eagerly.
+    """
+
+    def __init__(self, stacks, half_window, strides=(1, 1), alpha=0.001, ps_threshold=0.25, use_evd=False,
+                 compute_crlb=True, reference_idx=0, forms=None, graph=True):
+        self.stacks = list(stacks)
+        for z in self.stacks:
+            if not (D.is_device_tensor(z) and z.is_complex() and z.dim() == 3 and z.is_contiguous()):
+                raise ValueError("PhaseLinkBatch needs contiguous 3-D complex CUDA tensors")
+        self.hw = tuple(int(v) for v in half_window)
+        self.st = tuple(int(v) for v in strides)
+        self.alpha, self.thr = float(alpha), float(ps_threshold)
+        self.use_evd, self.crlb, self.ref = bool(use_evd), bool(compute_crlb), int(reference_idx)
+        depths = [int(z.shape[0]) for z in self.stacks]
+        self.forms = dict(forms) if forms is not None else tune_forms(depths, self.hw, self.st)
+        self.graph_enabled = bool(graph)
+        self._graph = None
+        self._outs = None
+        self._calls = None  # per stack: (params, workspace tensor)
+
+    def _enqueue(self):
+        """Enqueue every stack's pipeline on the current stream; returns the outputs."""
+        torch = D.require_cuda()
+        lib = _lib.load()
+        outs, calls = [], []
+        hy, hx = self.hw
+        sy, sx = self.st
+        for z in self.stacks:
+            n, rows, cols = (int(v) for v in z.shape)
+            mean, disp, ps = calc_ps_block(z.abs(), self.thr, n)
+            nb = estimate_neighbors(halfwin_rowcol=self.hw, alpha=self.alpha, strides=self.st, mean=mean,
+                                    var=(disp * mean) ** 2, nslc=n)
+            orow, ocol = rows // sy, cols // sx
+            prm = _lib.PlParams(nslc=n, rows=rows, cols=cols, hy=hy, hx=hx, sy=sy, sx=sx,
+                                use_evd=int(self.use_evd), beta=0.0, zero_correlation_threshold=0.0,
+                                reference_idx=self.ref, mask_input_ps=0, use_max_ps=1, use_slc_amp=0,
+                                baseline_lag=0, first_real_slc_idx=0, compute_crlb=int(self.crlb),
+                                cov_form=_form_code(self.forms.get(n, "tensor")))
+            o = {
+                "cpx": torch.empty((n, orow, ocol), dtype=torch.complex64, device=z.device),
+                "tc": torch.empty((orow, ocol), dtype=torch.float32, device=z.device),
+                "cnt": torch.empty((orow, ocol), dtype=torch.int32, device=z.device),
+                "eig": torch.empty((orow, ocol), dtype=torch.float32, device=z.device),
+                "est": torch.empty((orow, ocol), dtype=torch.uint8, device=z.device),
+                "crlb": torch.empty((n, orow, ocol), dtype=torch.float32, device=z.device),
+                "clos": torch.empty((orow, ocol, max(n - 2, 1)), dtype=torch.float32, device=z.device),
+            }
+            ws = torch.empty(max(int(lib.dpl_phase_link_workspace_size(prm)), 256), dtype=torch.uint8,
+                             device=z.device)
+            inp = _lib.PlInputs(slc=D.ptr(z), nodata_mask=None, ps_mask=D.ptr(ps), neighbors=D.ptr(nb),
+                                avg_mag=D.ptr(mean))
+            outp = _lib.PlOutputs(cpx_phase=D.ptr(o["cpx"]), temp_coh=D.ptr(o["tc"]), shp_counts=D.ptr(o["cnt"]),
+                                  eigenvalues=D.ptr(o["eig"]), estimator=D.ptr(o["est"]),
+                                  crlb_std_dev=D.ptr(o["crlb"]),
+                                  closure_phases=D.ptr(o["clos"]) if n > 2 else None)
+            _lib.check(lib.dpl_phase_link_async(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle()),
+                       "dpl_phase_link_async")
+            o["_keep"] = (mean, disp, ps, nb)  # inputs of the captured kernels stay allocated
+            outs.append(o)
+            calls.append((prm, ws))
+        return outs, calls
+
+    def _check(self, calls):
+        lib = _lib.load()
+        for prm, ws in calls:
+            _lib.check(lib.dpl_phase_link_status(prm, D.ptr(ws), ws.numel(), D.stream_handle()),
+                       "dpl_phase_link")
+
+    def run(self):
+        """Process every stack; returns a list of ``PhaseLinkOutput`` (CUDA tensors)."""
+        torch = D.require_cuda()
+        if not self.graph_enabled:
+            outs, calls = self._enqueue()
+            self._check(calls)
+            return [self._output(o) for o in outs]
+        if self._graph is None:
+            # eager warm-up (kernel attributes, libraries), then capture on a side stream
+            outs, calls = self._enqueue()
+            self._check(calls)
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s), torch.cuda.graph(g, stream=s):
+                self._outs, self._calls = self._enqueue()
+            torch.cuda.current_stream().wait_stream(s)
+            self._graph = g
+        self._graph.replay()
+        self._check(self._calls)
+        return [self._output(o) for o in self._outs]
+
+    @staticmethod
+    def _output(o):
+        return PhaseLinkOutput(o["cpx"], o["tc"], o["cnt"], o["eig"], o["est"], o["crlb"], o["clos"])

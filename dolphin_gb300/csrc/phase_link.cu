@@ -670,8 +670,9 @@ extern "C" size_t dpl_phase_link_workspace_size(const dpl_pl_params* p) {
                                nullptr);
 }
 
-extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
-                                     void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
+// Enqueues the whole pipeline on `stream` without synchronising.
+static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
+                             void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
     if (!prm || !in || !out) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link: null argument");
     const dpl_pl_params& P = *prm;
     dpl_status st = validate_common(P.nslc, P.rows, P.cols, P.hy, P.hx, P.sy, P.sx);
@@ -766,6 +767,12 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
         st = check_launch("k_post");
         if (st != DPL_OK) return st;
     }
+    return DPL_OK;
+}
+
+// Waits for `stream`, then reports what the enqueued pipeline left in the workspace: an
+// all-NaN SLC (the reference's message), an undefined PS brightness, a device timeout.
+static dpl_status pl_check(int n, const PlWorkspace& w, cudaStream_t s) {
     int host_status[2] = {0, 0};
     unsigned int host_valid[2] = {0, 0};
     DPL_CUDA_TRY(cudaMemcpyAsync(host_status, w.status, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -786,6 +793,29 @@ extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inpu
         return fail(DPL_ERR_INVALID_ARGUMENT, "a PS look window has no finite brightness (avg_mag is NaN at its PS pixels)");
     if (host_status[0] != 0) return fail((dpl_status)host_status[0], "device-side error");
     return DPL_OK;
+}
+
+extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
+                                     void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
+    dpl_status st = pl_enqueue(prm, in, out, workspace, workspace_bytes, stream);
+    if (st != DPL_OK) return st;
+    return dpl_phase_link_status(prm, workspace, workspace_bytes, stream);
+}
+
+extern "C" dpl_status dpl_phase_link_async(const dpl_pl_params* prm, const dpl_pl_inputs* in,
+                                           const dpl_pl_outputs* out, void* workspace, size_t workspace_bytes,
+                                           dpl_stream_t stream) {
+    return pl_enqueue(prm, in, out, workspace, workspace_bytes, stream);
+}
+
+extern "C" dpl_status dpl_phase_link_status(const dpl_pl_params* prm, void* workspace, size_t workspace_bytes,
+                                            dpl_stream_t stream) {
+    if (!prm || !workspace) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link_status: null argument");
+    if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
+    PlWorkspace w;
+    pl_workspace_layout(prm->nslc, prm->rows, prm->cols, std::max(1, prm->sy), std::max(1, prm->sx), prm->cov_form,
+                        (char*)workspace, &w);
+    return pl_check((int)prm->nslc, w, (cudaStream_t)stream);
 }
 
 extern "C" size_t dpl_covariance_workspace_size(int64_t nslc, int64_t rows, int64_t cols) {

@@ -49,6 +49,10 @@ class StackConfig:
     # pixels follow the model with gamma0 = disk_gamma0 instead
     disk_gamma0: float | None = None
     disk_radius: float = 0.125
+    # optional outlier pixels: with probability outlier_frac * col / cols a pixel's
+    # amplitudes follow LogNormal(0, outlier_sigma) instead (varies the SHP counts)
+    outlier_frac: float = 0.0
+    outlier_sigma: float = 1.0
 
 
 def coherence_model(nslc, gamma0, gamma_inf, tau, acq_interval=12.0):
@@ -93,6 +97,10 @@ def make_stack(cfg: StackConfig = StackConfig(), return_truth=False):
         disk = _disk_mask(cfg)
         x[:, disk] = (Ld @ w)[:, disk.ravel()]
     amp = rng.lognormal(mean=0.0, sigma=cfg.amp_sigma, size=(n, rows, cols))
+    if cfg.outlier_frac > 0:
+        prob = cfg.outlier_frac * np.arange(cols)[None, :] / cols
+        out = rng.random((rows, cols)) < prob
+        amp[:, out] = rng.lognormal(mean=0.0, sigma=cfg.outlier_sigma, size=(n, int(out.sum())))
     phi = _defo_phase(n, rows, cols, cfg.defo_peak)
     z = amp * np.exp(1j * phi) * x
     ps = rng.random((rows, cols)) < cfg.ps_frac
@@ -140,6 +148,11 @@ def make_stack_torch(cfg: StackConfig, device="cuda", rows_chunk=1024):
             xd = (Ldc @ w).reshape(n, r1 - r0, cols)
             x = torch.where(disk[None], xd, x)
         amp = torch.exp(cfg.amp_sigma * torch.randn((n, r1 - r0, cols), generator=g, device=device))
+        if cfg.outlier_frac > 0:
+            prob = cfg.outlier_frac * torch.arange(cols, device=device)[None, :] / cols
+            out_px = torch.rand((r1 - r0, cols), generator=g, device=device) < prob
+            amp_o = torch.exp(cfg.outlier_sigma * torch.randn((n, r1 - r0, cols), generator=g, device=device))
+            amp = torch.where(out_px[None], amp_o, amp)
         phi = phi_full[:, r0:r1]
         z = amp * torch.polar(torch.ones_like(phi), phi) * x
         ps = torch.rand((r1 - r0, cols), generator=g, device=device) < cfg.ps_frac

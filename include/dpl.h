@@ -138,6 +138,17 @@ dpl_status dpl_phase_link(const dpl_pl_params* params, const dpl_pl_inputs* inpu
                           const dpl_pl_outputs* outputs, void* workspace,
                           size_t workspace_bytes, dpl_stream_t stream);
 
+/* The two halves of dpl_phase_link (no reference counterpart: the reference runs
+ * synchronously).  dpl_phase_link_async enqueues the pipeline and returns without
+ * synchronising, so a sequence of calls (e.g. several ministacks) can be captured in a
+ * CUDA graph; the per-call status stays in the workspace.  dpl_phase_link_status
+ * synchronises `stream` and reports that status exactly as dpl_phase_link does. */
+dpl_status dpl_phase_link_async(const dpl_pl_params* params, const dpl_pl_inputs* inputs,
+                                const dpl_pl_outputs* outputs, void* workspace,
+                                size_t workspace_bytes, dpl_stream_t stream);
+dpl_status dpl_phase_link_status(const dpl_pl_params* params, void* workspace,
+                                 size_t workspace_bytes, dpl_stream_t stream);
+
 /* ---------------------------------------------------------------------------------
  * Stage entry points (used to check each stage against the oracle).
  * ------------------------------------------------------------------------------- */
