@@ -492,25 +492,29 @@ static dpl_status launch_pixel_pass(const PixArgs& a, cudaStream_t s) {
     return go(k_pixel<2, MODE, kLU>);
 }
 
-// Register-resident solve pass for n <= 32 (8 warps per CTA, one pixel per warp).
+// Register-resident solve pass for n <= 64: 8 warps per CTA, one pixel per warp
+// (n <= 32) or per pair of warps (n <= 64).
 static dpl_status launch_solve_reg(const PixArgs& a, cudaStream_t s) {
     const RegLayout L = make_reg_layout(a.n);
     const int warps = 8;
-    const size_t smem = (size_t)warps * L.bytes + (size_t)a.n * (a.n - 1) / 2 * sizeof(uint32_t);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    auto go = [&](auto kernel) -> dpl_status {
+    auto go = [&](auto kernel, int group_warps) -> dpl_status {
+        const int groups = warps / group_warps;
+        const size_t smem = (size_t)groups * L.bytes + (size_t)a.n * (a.n - 1) / 2 * sizeof(uint32_t);
+        if (smem > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "register solver: shared memory exceeds the SM limit");
         DPL_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
         DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, warps * 32, smem));
         const int64_t resident = (int64_t)std::max(1, per_sm) * std::max(1, sms);
-        const int64_t grid = std::min<int64_t>((a.npix + warps - 1) / warps, resident * 8);
+        const int64_t grid = std::min<int64_t>((a.npix + groups - 1) / groups, resident * 8);
         kernel<<<(unsigned)std::max<int64_t>(grid, 1), warps * 32, smem, s>>>(a, L);
         return check_launch("k_solve_reg");
     };
-    if (a.n <= 16) return go(k_solve_reg<16>);
-    return go(k_solve_reg<32>);
+    if (a.n <= 16) return go(k_solve_reg<16, 1>, 1);
+    if (a.n <= 32) return go(k_solve_reg<32, 1>, 1);
+    return go(k_solve_reg<64, 2>, 2);
 }
 
 // Main pass (Cholesky inverse iteration) and, for the pixels it lists, the LU pass.
@@ -523,7 +527,7 @@ static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr) {
     DPL_CUDA_TRY(cudaMemsetAsync(fb, 0, sizeof(int), s));
     a.fb_count = fb;
     a.fb_list = fb + 64;
-    dpl_status st = MODE == kSolveOnly && a.n <= 32 ? launch_solve_reg(a, s) : launch_pixel_pass<MODE, false>(a, s);
+    dpl_status st = MODE == kSolveOnly && a.n <= 64 ? launch_solve_reg(a, s) : launch_pixel_pass<MODE, false>(a, s);
     if (st != DPL_OK) return st;
     PixArgs b = a;
     fill_pix_layout(b, a.n, 2 * a.hx + 1, true);

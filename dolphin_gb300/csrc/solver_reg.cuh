@@ -1,5 +1,6 @@
-// Register-resident per-pixel solver for N <= K (K = 16 or 32): one warp per pixel,
-// lane i owns row i of each matrix in registers.
+// Register-resident per-pixel solver for N <= K: a group of G warps solves one pixel
+// (K = 16 or 32 with one warp, K = 64 with two warps); thread i of the group owns row i
+// of each matrix in registers.
 //
 // Same algorithms, iteration rules and outputs as solve_pixel (solver.cuh), laid out
 // for the register file instead of shared memory:
@@ -23,12 +24,12 @@
 
 namespace dpl {
 
-// Shared memory per warp: full Hermitian C (n x ld, ld odd: a lane-per-row access of
-// one column is conflict-free), |Gamma|^{-1} (n x ld floats), a 32-entry broadcast
-// buffer and a 32-entry vector buffer.
+// Shared memory per pixel group: full Hermitian C (n x ld, ld odd: a thread-per-row
+// access of one column is conflict-free), |Gamma| / |Gamma|^{-1} (n x ld floats), a
+// 64-entry broadcast buffer, a 64-entry vector buffer and reduction slots.
 struct RegLayout {
     int ld;
-    size_t off_C, off_G, off_b, off_w, bytes;
+    size_t off_C, off_G, off_b, off_w, off_x, bytes;
 };
 
 inline RegLayout make_reg_layout(int n) {
@@ -42,23 +43,70 @@ inline RegLayout make_reg_layout(int n) {
     };
     L.off_C = take((size_t)n * L.ld * sizeof(cfloat));
     L.off_G = take((size_t)n * L.ld * sizeof(float));
-    L.off_b = take(32 * sizeof(cfloat));
-    L.off_w = take(32 * sizeof(cfloat));
+    L.off_b = take(64 * sizeof(cfloat));
+    L.off_w = take(64 * sizeof(cfloat));
+    L.off_x = take(16 * sizeof(float));
     L.bytes = align_up(o, 128);
     return L;
 }
 
-// Real symmetric sweep over indices 0..n-1 of the matrix whose row `lane` is g; on
-// success g holds row `lane` of -A^{-1}.  Returns false (uniformly) if any pivot was
+// A pixel group of G warps (G = 1 or 2): row index, synchronisation and reductions.
+template <int G>
+struct Grp {
+    int gl;      // thread (= row) index within the group, 0 .. 32G - 1
+    int lane;    // lane within its warp
+    int wig;     // warp within the group
+    int bar;     // named barrier of the group (G == 2)
+    float* x;    // reduction slots (shared memory, 16 floats)
+
+    __device__ __forceinline__ void sync() const {
+        if (G == 1) __syncwarp();
+        else asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(32 * G) : "memory");
+    }
+    // sum over the group, the same value in every thread
+    __device__ __forceinline__ float sum(float v) const {
+        v = warp_sum(v);
+        if (G == 1) return v;
+        if (lane == 0) x[wig] = v;
+        sync();
+        const float r = x[0] + x[1];
+        sync();
+        return r;
+    }
+    __device__ __forceinline__ bool any(bool v) const {
+        v = warp_any(v);
+        if (G == 1) return v;
+        if (lane == 0) x[2 + wig] = v ? 1.f : 0.f;
+        sync();
+        const bool r = x[2] + x[3] > 0.f;
+        sync();
+        return r;
+    }
+    // value of thread k (uniform k)
+    __device__ __forceinline__ cfloat bcast(cfloat v, int k) const {
+        if (G == 1) return shfl_c(v, k);
+        if (gl == k) {
+            x[4] = v.re;
+            x[5] = v.im;
+        }
+        sync();
+        const cfloat r = cmake(x[4], x[5]);
+        sync();
+        return r;
+    }
+};
+
+// Real symmetric sweep over indices 0..n-1 of the matrix whose row `gl` is g; on
+// success g holds row `gl` of -A^{-1}.  Returns false (uniformly) if any pivot was
 // <= 0 (the remaining steps then run on meaningless values, without branching).
-template <int K>
-__device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int lane) {
-    bool bad = false;  // uniform: every lane reads the same pivot
+template <int K, int G>
+__device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, const Grp<G>& gr) {
+    bool bad = false;  // uniform: every thread reads the same pivot
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
-        __syncwarp();
-        if (lane < K) buf[(lane - k) & (K - 1)] = g[0];  // A[lane][k] (= A[k][lane])
-        __syncwarp();
+        gr.sync();
+        if (gr.gl < K) buf[(gr.gl - k) & (K - 1)] = g[0];  // A[row][k] (= A[k][row])
+        gr.sync();
         float r[K];
         const float4* b4 = reinterpret_cast<const float4*>(buf);
 #pragma unroll
@@ -72,9 +120,9 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int la
         const float p = r[0];
         bad |= !(p > 0.f);
         const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
-        const bool me = lane == k;
+        const bool me = gr.gl == k;
         // rows i != k: a_ij - (a_ik / p) a_kj; row k: a_kj / p, written as
-        // a_kj - (1 - 1/p) a_kj so that every lane runs the same FMA
+        // a_kj - (1 - 1/p) a_kj so that every thread runs the same FMA
         const float t = me ? 1.f - ip : g[0] * ip;
         const float last = me ? -ip : g[0] * ip;
 #pragma unroll
@@ -88,23 +136,23 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, int la
         for (int s = 0; s < K - 1; ++s) g[s] = g[s + 1];
         g[K - 1] = t0;
     }
-    __syncwarp();
+    gr.sync();
     return !bad;
 }
 
-// Hermitian sweep: on success a holds row `lane` of -A^{-1}.  False if a pivot was <= 0.
-template <int K>
-__device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, int lane) {
-    bool bad = false;  // uniform: every lane reads the same pivot
+// Hermitian sweep: on success a holds row `gl` of -A^{-1}.  False if a pivot was <= 0.
+template <int K, int G>
+__device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, const Grp<G>& gr) {
+    bool bad = false;  // uniform: every thread reads the same pivot
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
-        __syncwarp();
-        if (lane < K) buf[(lane - k) & (K - 1)] = a[0];  // A[lane][k] = conj(A[k][lane])
-        __syncwarp();
+        gr.sync();
+        if (gr.gl < K) buf[(gr.gl - k) & (K - 1)] = a[0];  // A[row][k] = conj(A[k][row])
+        gr.sync();
         const float p = buf[0].re;
         bad |= !(p > 0.f);
         const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
-        const bool me = lane == k;
+        const bool me = gr.gl == k;
         const cfloat t = me ? cmake(1.f - ip, 0.f) : cscale(a[0], ip);
         const cfloat last = me ? cmake(-ip, 0.f) : cscale(a[0], ip);
         const float4* b4 = reinterpret_cast<const float4*>(buf);
@@ -124,16 +172,16 @@ __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, in
         for (int s = 0; s < K - 1; ++s) a[s] = a[s + 1];
         a[K - 1] = t0;
     }
-    __syncwarp();
+    gr.sync();
     return !bad;
 }
 
-// y_lane = sum_j h[j] x_j (row `lane` of a matrix in registers); x published in vb
-template <int K>
-__device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloat* vb, int lane) {
-    __syncwarp();
-    vb[lane] = x;
-    __syncwarp();
+// y_row = sum_j h[j] x_j (row `gl` of a matrix in registers); x published in vb
+template <int K, int G>
+__device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloat* vb, const Grp<G>& gr) {
+    gr.sync();
+    vb[gr.gl] = x;
+    gr.sync();
     const float4* v4 = reinterpret_cast<const float4*>(vb);
     cfloat acc0 = cmake(0.f, 0.f), acc1 = cmake(0.f, 0.f);
 #pragma unroll
@@ -146,9 +194,10 @@ __device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloa
 }
 
 // Asynchronous copy of one pixel's planar coherence (count floats) into shared memory.
-__device__ __forceinline__ void r_prefetch(float* dst, const float* src, int count, int lane) {
-    __syncwarp();
-    for (int e = lane; e < count; e += 32)
+template <int G>
+__device__ __forceinline__ void r_prefetch(float* dst, const float* src, int count, const Grp<G>& gr) {
+    gr.sync();
+    for (int e = gr.gl; e < count; e += 32 * G)
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + e)),
                      "l"(src + e)
                      : "memory");
@@ -157,14 +206,14 @@ __device__ __forceinline__ void r_prefetch(float* dst, const float* src, int cou
 
 // Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps
 // (the reference's while-loop: iteration count starts at 1, stops below 50).
-template <class Op>
-__device__ __forceinline__ cfloat r_iterate(cfloat v, Op&& op) {
+template <int G, class Op>
+__device__ __forceinline__ cfloat r_iterate(cfloat v, const Grp<G>& gr, Op&& op) {
     float diff = 1.f;
     for (int it = 1; diff > 1e-5f && it < 50; ++it) {
         cfloat x = op(v);
-        const float inv = 1.f / sqrtf(warp_sum(cabs2(x)));
+        const float inv = 1.f / sqrtf(gr.sum(cabs2(x)));
         x = cscale(x, inv);
-        diff = sqrtf(warp_sum(cabs2(csub(x, v))));
+        diff = sqrtf(gr.sum(cabs2(csub(x, v))));
         v = x;
     }
     return v;
@@ -173,21 +222,21 @@ __device__ __forceinline__ cfloat r_iterate(cfloat v, Op&& op) {
 // Full solve for one pixel whose Hermitian coherence matrix is in Cf (n x ld, both
 // triangles).  A pixel whose shifted EMI matrix is not positive definite is appended
 // to a.fb_list and left for the LU pass.  Once Gs is no longer needed, the planar
-// coherence of the warp's next pixel (`next`, if any) is prefetched into it.
-template <int K>
+// coherence of the group's next pixel (`next`, if any) is prefetched into it.
+template <int K, int G>
 __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, float* Gs, int ld, cfloat* cb,
-                                cfloat* wb, const uint32_t* ptab, const float* next, int lane) {
-    const int n = a.n;
-    const bool row = lane < n;
-    const cfloat* Ci = Cf + (row ? lane : 0) * ld;
-    if (a.closure && lane < n - 2) {
-        const cfloat c = cmulc(cmul(Cf[lane * ld + lane + 1], Cf[(lane + 1) * ld + lane + 2]), Cf[lane * ld + lane + 2]);
-        a.closure[p * (n - 2) + lane] = atan2f(c.im, c.re);
+                                cfloat* wb, const uint32_t* ptab, const float* next, const Grp<G>& gr) {
+    const int n = a.n, me = gr.gl;
+    const bool row = me < n;
+    const cfloat* Ci = Cf + (row ? me : 0) * ld;
+    if (a.closure && me < n - 2) {
+        const cfloat c = cmulc(cmul(Cf[me * ld + me + 1], Cf[(me + 1) * ld + me + 2]), Cf[me * ld + me + 2]);
+        a.closure[p * (n - 2) + me] = atan2f(c.im, c.re);
     }
     // |Gamma| + 1e-6 I -> -|Gamma|^{-1} (round 0), then the CRLB's Fisher matrix
     // FIM = 2L (Gamma o Gamma^{-1} - I), row/col `ref` -> identity, + 1e-6 I (round 1).
     // Gs holds |Gamma| during round 0 and |Gamma|^{-1} afterwards.
-    float* Gi = Gs + (row ? lane : 0) * ld;
+    float* Gi = Gs + (row ? me : 0) * ld;
     const int ref = a.crlb_ref;
     bool inv_nan = true;
     bool crlb_ok = false;
@@ -198,20 +247,20 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         for (int j = 0; j < K; ++j) {
             float x = 0.f;
             if (row && j < n) {
-                x = s_gamma(a, Ci[j], j == lane);
+                x = s_gamma(a, Ci[j], j == me);
                 Gi[j] = x;
-                if (j == lane) x = fadd(x, 1e-6f);
+                if (j == me) x = fadd(x, 1e-6f);
             }
             g[j] = x;
         }
 #pragma unroll 1
         for (int round = 0; round < 2; ++round) {
-            const bool ok = r_sweep<K>(g, n, reinterpret_cast<float*>(cb), lane);
+            const bool ok = r_sweep<K, G>(g, n, reinterpret_cast<float*>(cb), gr);
             if (round == 1) {
                 crlb_ok = ok;
 #pragma unroll
                 for (int j = 0; j < K; ++j)
-                    if (j == lane) dg = g[j];
+                    if (j == me) dg = g[j];
                 break;
             }
             inv_nan = !ok;
@@ -219,7 +268,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
                 bool bad = false;
 #pragma unroll
                 for (int j = 0; j < K; ++j) bad |= isnan(g[j]);
-                inv_nan = warp_any(bad);
+                inv_nan = gr.any(bad);
             }
             // keep |Gamma|^{-1} and build the FIM in place of it
 #pragma unroll
@@ -227,11 +276,11 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
                 const float ginv = -g[j];
                 float x = 0.f;
                 if (row && j < n) {
-                    if (lane == ref || j == ref) {
-                        x = j == lane ? 1.f : 0.f;
+                    if (me == ref || j == ref) {
+                        x = j == me ? 1.f : 0.f;
                     } else {
-                        x = fmul(a.crlb_factor, fsub(fmul(Gi[j], ginv), j == lane ? 1.f : 0.f));
-                        if (j == lane) x = fadd(x, 1e-6f);
+                        x = fmul(a.crlb_factor, fsub(fmul(Gi[j], ginv), j == me ? 1.f : 0.f));
+                        if (j == me) x = fadd(x, 1e-6f);
                     }
                     Gi[j] = ginv;
                 }
@@ -241,7 +290,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         }
     }
     const bool evd = a.use_evd || inv_nan;
-    if (row) a.crlb[p * n + lane] = !a.compute_crlb || lane == ref ? 0.f : (crlb_ok ? sqrtf(-dg) : nanf(""));
+    if (row) a.crlb[p * n + me] = !a.compute_crlb || me == ref ? 0.f : (crlb_ok ? sqrtf(-dg) : nanf(""));
 
     cfloat v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
     float lambda;
@@ -252,35 +301,35 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
             cfloat x = cmake(0.f, 0.f);
             if (row && j < n) {
                 x = cscale(Ci[j], Gi[j]);
-                if (j == lane) x.re = fsub(x.re, 0.99f);
+                if (j == me) x.re = fsub(x.re, 0.99f);
             }
             am[j] = x;
         }
-        if (!r_sweep_c<K>(am, n, cb, lane)) {
-            if (lane == 0) a.fb_list[atomicAdd(a.fb_count, 1)] = (int)p;
-            if (next) r_prefetch(Gs, next, n * n, lane);
-            __syncwarp();
+        if (!r_sweep_c<K, G>(am, n, cb, gr)) {
+            if (me == 0) a.fb_list[atomicAdd(a.fb_count, 1)] = (int)p;
+            if (next) r_prefetch<G>(Gs, next, n * n, gr);
+            gr.sync();
             return;
         }
         // am = -(A - 0.99 I)^{-1}: x <- (A - 0.99 I)^{-1} v = -(am v)
-        v = r_iterate(v, [&](cfloat x) {
-            const cfloat y = r_matvec<K>(am, x, wb, lane);
+        v = r_iterate<G>(v, gr, [&](cfloat x) {
+            const cfloat y = r_matvec<K, G>(am, x, wb, gr);
             return cmake(-y.re, -y.im);
         });
         // lambda = Re v^H A v, A_ij = |Gamma|^{-1}_ij C_ij
-        __syncwarp();
-        wb[lane] = v;
-        __syncwarp();
+        gr.sync();
+        wb[me] = v;
+        gr.sync();
         cfloat acc = cmake(0.f, 0.f);
         if (row) {
             for (int j = 0; j < n; ++j) acc = cfma(acc, cscale(Ci[j], Gi[j]), wb[j]);
         }
-        if (next) r_prefetch(Gs, next, n * n, lane);
-        const float n2 = warp_sum(cabs2(v));
-        lambda = warp_sum(v.re * acc.re + v.im * acc.im);
+        if (next) r_prefetch<G>(Gs, next, n * n, gr);
+        const float n2 = gr.sum(cabs2(v));
+        lambda = gr.sum(v.re * acc.re + v.im * acc.im);
         v = cscale(v, sqrtf((float)n) / sqrtf(n2));
     } else {
-        if (next) r_prefetch(Gs, next, n * n, lane);
+        if (next) r_prefetch<G>(Gs, next, n * n, gr);
         cfloat h[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
@@ -291,27 +340,26 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
             }
             h[j] = x;
         }
-        v = r_iterate(v, [&](cfloat x) { return r_matvec<K>(h, x, wb, lane); });
-        const cfloat y = r_matvec<K>(h, v, wb, lane);
-        lambda = warp_sum(v.re * y.re + v.im * y.im);
+        v = r_iterate<G>(v, gr, [&](cfloat x) { return r_matvec<K, G>(h, x, wb, gr); });
+        const cfloat y = r_matvec<K, G>(h, v, wb, gr);
+        lambda = gr.sum(v.re * y.re + v.im * y.im);
     }
     // reference to reference_idx
-    const cfloat rot = cconj(fphasor(shfl_c(v, a.ref_idx)));
+    const cfloat rot = cconj(fphasor(gr.bcast(v, a.ref_idx)));
     v = cmul(v, rot);
-    if (row) a.vout[p * n + lane] = v;
-    if (lane == 0) {
+    if (row) a.vout[p * n + me] = v;
+    if (me == 0) {
         a.eig[p] = lambda;
         a.est[p] = evd ? 0 : 1;
     }
     // temporal coherence over pairs c < r (ptab: the lower pairs r | c << 16, row by
     // row): conj(phasor(C_rc) w_c conj(w_r))
-    __syncwarp();
-    wb[lane] = fphasor(v);
-    __syncwarp();
-    float sre = 0.f, sim = 0.f;
-    int cnt = 0;
+    gr.sync();
+    wb[me] = fphasor(v);
+    gr.sync();
+    float sre = 0.f, sim = 0.f, cnt = 0.f;
     const int npairs = n * (n - 1) / 2;
-    for (int e = lane; e < npairs; e += 32) {
+    for (int e = me; e < npairs; e += 32 * G) {
         const uint32_t rc = ptab[e];
         const int r = rc & 0xffff, c = rc >> 16;
         const cfloat u = fphasor(Cf[r * ld + c]);
@@ -319,35 +367,41 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         if (!cisnan(t)) {
             sre += t.re;
             sim += t.im;
-            ++cnt;
+            cnt += 1.f;
         }
     }
-    sre = warp_sum(sre);
-    sim = warp_sum(sim);
-    cnt = warp_sum_int(cnt);
-    if (lane == 0) {
-        const float fc = (float)cnt;
-        const float tc = hypotf(sre / fc, sim / fc);
+    sre = gr.sum(sre);
+    sim = gr.sum(sim);
+    cnt = gr.sum(cnt);  // exact: at most 2016 pairs
+    if (me == 0) {
+        const float tc = hypotf(sre / cnt, sim / cnt);
         a.tcoh[p] = isfinite(tc) ? tc : 0.f;
     }
-    __syncwarp();
+    gr.sync();
 }
 
-// Solve-only pass over all pixels with the register solver (n <= K).  The coherence
-// comes planar (diagonal, then (Re, Im) of the lower pair (i, j), i > j, at
-// o = i(i-1)/2 + j)
-// or as full (npix, n, n) matrices of which the lower triangle is read.
-template <int K>
-__global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
+// Solve-only pass over all pixels with the register solver (n <= K), one pixel per
+// group of G warps.  The coherence comes planar (diagonal, then (Re, Im) of the
+// lower pair (i, j), i > j, at o = i(i-1)/2 + j) or as full (npix, n, n) matrices
+// of which the lower triangle is read.
+template <int K, int G>
+__global__ void __launch_bounds__(256, 3 - G) k_solve_reg(PixArgs a, RegLayout L) {
     extern __shared__ __align__(16) unsigned char reg_smem[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    unsigned char* base = reg_smem + warp * L.bytes;
+    const int warp = threadIdx.x >> 5, ngroups = (blockDim.x >> 5) / G;
+    const int group = warp / G;
+    Grp<G> gr;
+    gr.lane = threadIdx.x & 31;
+    gr.wig = warp - group * G;
+    gr.gl = gr.wig * 32 + gr.lane;
+    gr.bar = 1 + group;
+    unsigned char* base = reg_smem + group * L.bytes;
+    gr.x = reinterpret_cast<float*>(base + L.off_x);
     cfloat* Cf = reinterpret_cast<cfloat*>(base + L.off_C);
     float* Gs = reinterpret_cast<float*>(base + L.off_G);
     cfloat* cb = reinterpret_cast<cfloat*>(base + L.off_b);
     cfloat* wb = reinterpret_cast<cfloat*>(base + L.off_w);
-    uint32_t* ptab = reinterpret_cast<uint32_t*>(reg_smem + nwarps * L.bytes);  // shared by the CTA
-    const int n = a.n, ld = L.ld, lag = a.baseline_lag;
+    uint32_t* ptab = reinterpret_cast<uint32_t*>(reg_smem + ngroups * L.bytes);  // shared by the CTA
+    const int n = a.n, ld = L.ld, lag = a.baseline_lag, me = gr.gl;
     for (int o = threadIdx.x; o < n * (n - 1) / 2; o += blockDim.x) {
         int r = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = r(r-1)/2 + c, 0 <= c < r
         while (r * (r - 1) / 2 > o) --r;
@@ -355,38 +409,38 @@ __global__ void __launch_bounds__(256, 2) k_solve_reg(PixArgs a, RegLayout L) {
         ptab[o] = (uint32_t)r | ((uint32_t)(o - r * (r - 1) / 2) << 16);
     }
     __syncthreads();
-    const int64_t stride = (int64_t)gridDim.x * nwarps;
+    const int64_t stride = (int64_t)gridDim.x * ngroups;
     bool staged = false;  // Gs holds this pixel's planar coherence (prefetched)
-    for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += stride) {
-        __syncwarp();
+    for (int64_t p = (int64_t)blockIdx.x * ngroups + group; p < a.npix; p += stride) {
+        gr.sync();
         if (a.Cplanar) {
             if (staged) asm volatile("cp.async.wait_group 0;" ::: "memory");
-            __syncwarp();
+            gr.sync();
             const float* src = staged ? Gs : a.Cplanar + p * n * n;
-            if (lane < n) Cf[lane * ld + lane] = cmake(src[lane], 0.f);
+            if (me < n) Cf[me * ld + me] = cmake(src[me], 0.f);
             for (int i = 1; i < n; ++i) {
                 const int o = i * (i - 1) / 2;
-                if (lane < i) {
-                    cfloat c = cmake(src[n + 2 * (o + lane)], src[n + 2 * (o + lane) + 1]);
-                    if (lag > 0 && i - lane >= lag) c = cmake(0.f, 0.f);
-                    Cf[i * ld + lane] = c;
-                    Cf[lane * ld + i] = cconj(c);
+                if (me < i) {
+                    cfloat c = cmake(src[n + 2 * (o + me)], src[n + 2 * (o + me) + 1]);
+                    if (lag > 0 && i - me >= lag) c = cmake(0.f, 0.f);
+                    Cf[i * ld + me] = c;
+                    Cf[me * ld + i] = cconj(c);
                 }
             }
         } else {
             const cfloat* src = a.Cin + p * n * n;
             for (int i = 0; i < n; ++i) {
-                if (lane <= i) {
-                    cfloat c = src[i * n + lane];
-                    if (lag > 0 && i - lane >= lag) c = cmake(0.f, 0.f);
-                    Cf[i * ld + lane] = c;
-                    if (lane < i) Cf[lane * ld + i] = cconj(c);
+                if (me <= i) {
+                    cfloat c = src[i * n + me];
+                    if (lag > 0 && i - me >= lag) c = cmake(0.f, 0.f);
+                    Cf[i * ld + me] = c;
+                    if (me < i) Cf[me * ld + i] = cconj(c);
                 }
             }
         }
-        __syncwarp();
+        gr.sync();
         const float* next = a.Cplanar && p + stride < a.npix ? a.Cplanar + (p + stride) * n * n : nullptr;
-        solve_pixel_reg<K>(a, p, Cf, Gs, ld, cb, wb, ptab, next, lane);
+        solve_pixel_reg<K, G>(a, p, Cf, Gs, ld, cb, wb, ptab, next, gr);
         staged = next != nullptr;
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
