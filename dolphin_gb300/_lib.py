@@ -69,6 +69,14 @@ SIGNATURES = {
     "dpl_process_coherence_workspace_size": (_sz, [_i64]),
     "dpl_process_coherence": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _sz, _p]),
     "dpl_compress": (_i, [_p, _i64, _i64, _i64, _p, _i64, _i64, _i, _p, _i, _i, _p, _p]),
+    "dpl_process_coherence_warm": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _p,
+                                        _p, _sz, _p]),
+    "dpl_mlp_features": (_i, [_p, _i, _i64, _i, _p, _p]),
+    "dpl_gemm_f32": (_i, [_i, _i, _i, _p, _i64, _i64, _p, _i64, _i64, _p, _i64, _p, _f, _f, _i, _p]),
+    "dpl_relu_grad": (_i, [_p, _p, _i64, _p]),
+    "dpl_mse_grad": (_i, [_p, _p, _p, _i64, _p, _p]),
+    "dpl_colsum": (_i, [_p, _i, _i, _p, _p]),
+    "dpl_adam": (_i, [_p, _p, _p, _p, _i64, _f, _f, _f, _f, _i, _p]),
     "dpl_process_coherence_noalloc_max_pixels": (_i64, []),
     "dpl_process_coherence_noalloc": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p]),
     "dpl_kernel_timing": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

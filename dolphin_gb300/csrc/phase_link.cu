@@ -156,6 +156,8 @@ struct PixArgs {
     const uint32_t* nb_bits; // (out_rows, out_cols, wy, wpr) or null
     int wpr;
     const cfloat* Cin;       // solve-only input: (npix, n, n)
+    const cfloat* vstart;    // optional EMI starting vectors (npix, n); plain start when null
+    int16_t* iters;          // optional: eigen-iterations used per pixel (npix)
     const float* Cplanar;    // solve-only input, planar per pixel: diagonal | (Re, Im) per lower pair
     int use_evd, beta_on;
     float one_minus_beta, beta, zct;
@@ -910,6 +912,38 @@ extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int ns
     a.closure = nslc > 2 ? closure_phases : nullptr;
     if (!workspace || workspace_bytes < dpl_process_coherence_workspace_size(npix))
         return fail(DPL_ERR_WORKSPACE, "dpl_process_coherence: workspace too small");
+    return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream, reinterpret_cast<int*>(workspace));
+}
+
+extern "C" dpl_status dpl_process_coherence_warm(const float* C, int64_t npix, int nslc, int use_evd, double beta,
+                                                 double zero_correlation_threshold, int reference_idx,
+                                                 double num_looks, int first_real_slc_idx, int compute_crlb,
+                                                 const float* vstart, float* eig_vecs, float* eig_vals,
+                                                 uint8_t* estimator, float* crlb_std_dev, float* temp_coh,
+                                                 float* closure_phases, int16_t* iterations, void* workspace,
+                                                 size_t workspace_bytes, dpl_stream_t stream) {
+    if (npix < 0 || nslc <= 0) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_warm: bad shape");
+    if (nslc > kMaxNslc) return fail(DPL_ERR_UNSUPPORTED, "at most 64 SLCs per call are supported");
+    if (npix == 0) return DPL_OK;
+    if (!C || !eig_vecs || !eig_vals || !estimator || !crlb_std_dev || !temp_coh)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_warm: null pointer");
+    const int ref = norm_ref(reference_idx, nslc);
+    if (ref < 0 || ref >= nslc) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
+    if (!workspace || workspace_bytes < dpl_process_coherence_workspace_size(npix))
+        return fail(DPL_ERR_WORKSPACE, "dpl_process_coherence_warm: workspace too small");
+    PixArgs a{};
+    fill_pix_layout(a, nslc, 1);
+    a.npix = npix;
+    a.Cin = reinterpret_cast<const cfloat*>(C);
+    set_solver_params(a, use_evd, beta, zero_correlation_threshold, ref, num_looks, first_real_slc_idx, compute_crlb);
+    a.vstart = reinterpret_cast<const cfloat*>(vstart);
+    a.iters = iterations;
+    a.vout = reinterpret_cast<cfloat*>(eig_vecs);
+    a.eig = eig_vals;
+    a.est = estimator;
+    a.crlb = crlb_std_dev;
+    a.tcoh = temp_coh;
+    a.closure = nslc > 2 ? closure_phases : nullptr;
     return launch_pixel<kSolveOnly>(a, (cudaStream_t)stream, reinterpret_cast<int*>(workspace));
 }
 

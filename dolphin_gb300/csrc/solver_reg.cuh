@@ -205,9 +205,10 @@ __device__ __forceinline__ void r_prefetch(float* dst, const float* src, int cou
 }
 
 // Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps
-// (the reference's while-loop: iteration count starts at 1, stops below 50).
+// (the reference's while-loop: iteration count starts at 1, stops below 50).  Adds the
+// steps taken to `steps`; returns whether the stopping rule was met.
 template <int G, class Op>
-__device__ __forceinline__ cfloat r_iterate(cfloat v, const Grp<G>& gr, Op&& op) {
+__device__ __forceinline__ bool r_iterate(cfloat& v, const Grp<G>& gr, int& steps, Op&& op) {
     float diff = 1.f;
     for (int it = 1; diff > 1e-5f && it < 50; ++it) {
         cfloat x = op(v);
@@ -215,8 +216,9 @@ __device__ __forceinline__ cfloat r_iterate(cfloat v, const Grp<G>& gr, Op&& op)
         x = cscale(x, inv);
         diff = sqrtf(gr.sum(cabs2(csub(x, v))));
         v = x;
+        ++steps;
     }
-    return v;
+    return diff <= 1e-5f;
 }
 
 // Full solve for one pixel whose Hermitian coherence matrix is in Cf (n x ld, both
@@ -294,6 +296,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
 
     cfloat v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
     float lambda;
+    int steps = 0;
     if (!evd) {
         cfloat am[K];
 #pragma unroll
@@ -312,10 +315,25 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
             return;
         }
         // am = -(A - 0.99 I)^{-1}: x <- (A - 0.99 I)^{-1} v = -(am v)
-        v = r_iterate<G>(v, gr, [&](cfloat x) {
+        auto inv_op = [&](cfloat x) {
             const cfloat y = r_matvec<K, G>(am, x, wb, gr);
             return cmake(-y.re, -y.im);
-        });
+        };
+        bool warm = false;
+        if (a.vstart) {
+            // learned starting vector; plain EMI (constant start) if it is unusable or
+            // the iteration from it does not meet the stopping rule
+            const cfloat w0 = row ? a.vstart[p * n + me] : cmake(0.f, 0.f);
+            const float w2 = gr.sum(cabs2(w0));
+            if (w2 > 0.f && w2 <= 3.4e38f) {
+                v = cscale(w0, 1.f / sqrtf(w2));
+                warm = true;
+            }
+        }
+        if (!r_iterate<G>(v, gr, steps, inv_op) && warm) {
+            v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
+            r_iterate<G>(v, gr, steps, inv_op);
+        }
         // lambda = Re v^H A v, A_ij = |Gamma|^{-1}_ij C_ij
         gr.sync();
         wb[me] = v;
@@ -340,7 +358,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
             }
             h[j] = x;
         }
-        v = r_iterate<G>(v, gr, [&](cfloat x) { return r_matvec<K, G>(h, x, wb, gr); });
+        r_iterate<G>(v, gr, steps, [&](cfloat x) { return r_matvec<K, G>(h, x, wb, gr); });
         const cfloat y = r_matvec<K, G>(h, v, wb, gr);
         lambda = gr.sum(v.re * y.re + v.im * y.im);
     }
@@ -351,6 +369,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     if (me == 0) {
         a.eig[p] = lambda;
         a.est[p] = evd ? 0 : 1;
+        if (a.iters) a.iters[p] = (int16_t)steps;
     }
     // temporal coherence over pairs c < r (ptab: the lower pairs r | c << 16, row by
     // row): conj(phasor(C_rc) w_c conj(w_r))

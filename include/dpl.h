@@ -194,6 +194,48 @@ dpl_status dpl_compress(const float* slc, int64_t nslc, int64_t rows, int64_t co
                         int first_real_slc_idx, float* slc_mean, int has_reference,
                         int reference_idx, float* comp_slc, dpl_stream_t stream);
 
+/* ---------------------------------------------------------------------------------
+ * Learned EMI warm start (no counterpart in the reference, whose EMI inverse iteration
+ * starts from a constant vector, phase_link/_eigenvalues.py:139-205).
+ * ------------------------------------------------------------------------------- */
+
+/* dpl_process_coherence with optional per-pixel EMI starting vectors `vstart`
+ * ((npix, nslc) complex64, NULL: constant start).  A pixel whose iteration from its
+ * starting vector does not meet the stopping rule (|v_k+1 - v_k| <= 1e-5 within 49
+ * steps), or whose vector is zero or not finite, is iterated again from the constant
+ * start (plain EMI).  iterations: (npix) int16 out or NULL -- eigen-iterations used. */
+dpl_status dpl_process_coherence_warm(const float* C, int64_t npix, int nslc, int use_evd, double beta,
+                                      double zero_correlation_threshold, int reference_idx,
+                                      double num_looks, int first_real_slc_idx, int compute_crlb,
+                                      const float* vstart, float* eig_vecs, float* eig_vals,
+                                      uint8_t* estimator, float* crlb_std_dev, float* temp_coh,
+                                      float* closure_phases, int16_t* iterations, void* workspace,
+                                      size_t workspace_bytes, dpl_stream_t stream);
+
+/* Network input: |C_ij| of the nslc (nslc - 1) / 2 lower pairs (i > j, row by row) of
+ * each pixel's coherence, (npix, nslc(nslc-1)/2) float32.  layout 0: planar coherence
+ * (npix, nslc^2) floats (diagonal, then (Re, Im) per pair); layout 1: full (npix, nslc,
+ * nslc) complex64. */
+dpl_status dpl_mlp_features(const float* C, int nslc, int64_t npix, int layout, float* X,
+                            dpl_stream_t stream);
+
+/* C = act(alpha * op(A) op(B)^T + bias) (+ beta * C), fp32: element (i, k) of op(A) at
+ * A[i * sai + k * sak], (j, k) of op(B) at B[j * sbj + k * sbk], C row stride sci; bias
+ * per column j or NULL; act = ReLU if relu, else identity.  M x N x K. */
+dpl_status dpl_gemm_f32(int M, int N, int K, const float* A, int64_t sai, int64_t sak,
+                        const float* B, int64_t sbj, int64_t sbk, float* C, int64_t sci,
+                        const float* bias, float alpha, float beta, int relu, dpl_stream_t stream);
+
+/* Training-step kernels: dH *= (H > 0); dY = 2 (Y - T) / count with per-block partial
+ * sums of (Y - T)^2 in loss_parts[ceil(count / 256)]; column sums of an (M, N) matrix;
+ * Adam (step >= 1, bias-corrected). */
+dpl_status dpl_relu_grad(const float* H, float* dH, int64_t count, dpl_stream_t stream);
+dpl_status dpl_mse_grad(const float* Y, const float* T, float* dY, int64_t count,
+                        float* loss_parts, dpl_stream_t stream);
+dpl_status dpl_colsum(const float* X, int M, int N, float* out, dpl_stream_t stream);
+dpl_status dpl_adam(float* w, const float* grad, float* m, float* v, int64_t count, float lr,
+                    float b1, float b2, float eps, int step, dpl_stream_t stream);
+
 /* No counterpart in the reference: dpl_process_coherence without a caller-supplied
  * workspace, for callers that cannot allocate device memory per call (a C/GDAL-style
  * host that owns no device allocator and cannot size one, or a multi-stream pipeline

@@ -1,0 +1,105 @@
+"""Learned EMI warm start: the training kernels against the numpy oracle, and the gain.
+
+Run with ``-s`` to see the iteration counts with and without the warm start.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import mlp as M
+from parity import phase_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover - CPU container
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import dolphin_gb300 as dp  # noqa: E402
+from dolphin_gb300.learned import WarmStartMLP, make_training_set, process_coherence_warm  # noqa: E402
+from dolphin_gb300.simulate import StackConfig, make_stack_torch  # noqa: E402
+
+
+def _small(seed=3):
+    model = WarmStartMLP(nslc=4, hidden=(9, 6), seed=seed)  # 6 -> 9 -> 6 -> 8
+    rng = np.random.default_rng(seed)
+    X = rng.normal(size=(13, 6)).astype(np.float32)
+    T = rng.normal(size=(13, 8)).astype(np.float32)
+    st = model.state()
+    Ws = [st[f"W{k}"].astype(np.float64) for k in range(3)]
+    bs = [rng.normal(scale=0.1, size=w.shape[0]) for w in Ws]
+    model.load_state({**{f"W{k}": Ws[k] for k in range(3)}, **{f"b{k}": bs[k] for k in range(3)}})
+    bs = [b.astype(np.float32).astype(np.float64) for b in bs]
+    return model, X, T, Ws, bs
+
+
+def test_forward_and_gradients_match_oracle():
+    model, X, T, Ws, bs = _small()
+    Xd, Td = torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda()
+    outs = model.forward(Xd)
+    ref = M.forward(X.astype(np.float64), Ws, bs)
+    for o, r in zip(outs, ref):
+        np.testing.assert_allclose(o.cpu().numpy(), r, rtol=1e-5, atol=1e-6)
+    parts, count, grads = model.gradients(Xd, Td)
+    assert abs(float(parts.sum()) / count - M.mse(ref[-1], T)) < 1e-5
+    gW, gb = M.backward(X.astype(np.float64), T.astype(np.float64), Ws, bs)
+    for (w, b), rw, rb in zip(grads, gW, gb):
+        np.testing.assert_allclose(w.cpu().numpy(), rw, rtol=1e-4, atol=1e-6)
+        np.testing.assert_allclose(b.cpu().numpy(), rb, rtol=1e-4, atol=1e-6)
+
+
+def test_adam_step_matches_oracle():
+    model, X, T, Ws, bs = _small(4)
+    gW, gb = M.backward(X.astype(np.float64), T.astype(np.float64), Ws, bs)
+    model.train_step(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), lr=1e-2)
+    st = model.state()
+    for k in range(3):
+        w = Ws[k].copy()
+        M.adam_step(w, gW[k], np.zeros_like(w), np.zeros_like(w), 1e-2, 0.9, 0.999, 1e-8, 1)
+        np.testing.assert_allclose(st[f"W{k}"], w, rtol=1e-5, atol=1e-6)
+
+
+def test_features_layouts_match_oracle():
+    z = make_stack_torch(StackConfig(nslc=6, rows=12, cols=14, seed=5, ps_frac=0.0))
+    C = dp.estimate_stack_covariance(z, (2, 2)).reshape(-1, 6, 6).contiguous()
+    model = WarmStartMLP(nslc=6, hidden=(4,))
+    X = model.features(C, layout=1).cpu().numpy()
+    np.testing.assert_allclose(X, M.features(C.cpu().numpy()), rtol=1e-6)
+    # planar layout: diagonal, then (Re, Im) of the lower pairs row by row
+    Cn = C.cpu().numpy()
+    i, j = np.tril_indices(6, -1)
+    order = np.lexsort((j, i))
+    low = Cn[:, i[order], j[order]]
+    planar = np.concatenate([np.real(np.diagonal(Cn, axis1=1, axis2=2)),
+                             np.stack([low.real, low.imag], -1).reshape(len(Cn), -1)], 1).astype(np.float32)
+    Xp = model.features(torch.from_numpy(planar).cuda(), layout=0).cpu().numpy()
+    np.testing.assert_allclose(Xp, X, rtol=1e-6)
+
+
+def test_warm_start_saves_iterations():
+    n = 20
+    X, T = make_training_set(24000, nslc=n, tile=48)
+    model = WarmStartMLP(nslc=n, seed=0)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(0)
+    losses = []
+    for step in range(600):
+        idx = torch.randint(0, X.shape[0], (1024,), generator=gen, device="cuda")
+        losses.append(model.train_step(X[idx].contiguous(), T[idx].contiguous(), lr=1e-3))
+    assert np.mean(losses[-50:]) < 0.5 * np.mean(losses[:10])
+    # held-out stack
+    z = make_stack_torch(StackConfig(nslc=n, rows=96 + 10, cols=96 + 22, seed=4242, gamma0=0.6, gamma_inf=0.1,
+                                     tau=48.0, ps_frac=0.0))
+    C = dp.estimate_stack_covariance(z, (5, 11)).reshape(-1, n, n).contiguous()
+    v0, l0, e0, _c, t0, it0 = process_coherence_warm(C)
+    v1, l1, e1, _c, t1, it1 = process_coherence_warm(C, model)
+    emi = (e0 == 1).cpu().numpy()
+    it0, it1 = it0.cpu().numpy()[emi], it1.cpu().numpy()[emi]
+    fallback = float((it1 >= 50).mean())
+    print(f"[warm start] EMI pixels {emi.sum()}: mean iterations plain {it0.mean():.2f}, "
+          f"warm {it1.mean():.2f}, fallback {100 * fallback:.2f} %")
+    assert it1.mean() < 0.8 * it0.mean()
+    good = emi & (t0.cpu().numpy() > 0.3)
+    err = phase_err(v1.cpu().numpy()[good], v0.cpu().numpy()[good])
+    print(f"[warm start] phase difference to plain EMI: max {err.max():.2e}, p99 {np.percentile(err, 99):.2e} rad")
+    assert err.max() < 1e-3
