@@ -72,6 +72,7 @@ SIGNATURES = {
     "dpl_process_coherence_warm": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _p,
                                         _p, _sz, _p]),
     "dpl_mlp_features": (_i, [_p, _i, _i64, _i, _p, _p]),
+    "dpl_mlp_frame": (_i, [_p, _i, _i64, _p, _i, _p, _p]),
     "dpl_gemm_f32": (_i, [_i, _i, _i, _p, _i64, _i64, _p, _i64, _i64, _p, _i64, _p, _f, _f, _i, _p]),
     "dpl_relu_grad": (_i, [_p, _p, _i64, _p]),
     "dpl_mse_grad": (_i, [_p, _p, _p, _i64, _p, _p]),

@@ -3,8 +3,9 @@
 // iteration (no counterpart in the reference, whose iteration starts from a constant
 // vector, _eigenvalues.py:139-205; plain EMI stays the fallback).
 //
-//   k_mlp_features : planar coherence (diagonal, (Re, Im) per lower pair) -> |C_ij| of
-//                    the N(N-1)/2 lower pairs, the network input
+//   k_mlp_features : coherence (planar, or full complex) -> |C_ij| of the N(N-1)/2
+//                    lower pairs, the network input
+//   k_mlp_frame    : rotates vectors into / out of the frame of the data's phases
 //   k_gemm         : C = act(alpha * op(A) op(B)^T + bias) (+ beta C) in fp32, 64 x 64 tiles
 //                    staged through shared memory, 4 x 4 outputs per thread; any strides,
 //                    so the same kernel runs the forward pass and both backward products
@@ -33,6 +34,25 @@ __global__ void k_mlp_features(const float* __restrict__ C, int n, int64_t npix,
         src = C + ((p * n + i) * n + j) * 2;
     }
     X[e] = hypotf(src[0], src[1]);
+}
+
+// out_j = V_j * f_j (or * conj(f_j)), f_j = exp(i angle C_j0) the phase of SLC j's
+// interferogram with SLC 0 (f_0 = 1); C full (npix, N, N) complex, V and out (npix, N)
+// complex.  The network works in this frame: the data supply the phases, the network
+// the rest.
+__global__ void k_mlp_frame(const cfloat* __restrict__ C, int n, int64_t npix, const cfloat* __restrict__ V,
+                            int conj_frame, cfloat* __restrict__ out) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= npix * n) return;
+    const int64_t p = e / n;
+    const int j = (int)(e - p * n);
+    cfloat f = cmake(1.f, 0.f);
+    if (j > 0) {
+        const cfloat c = C[(p * n + j) * n];
+        const float m = hypotf(c.re, c.im);
+        if (m > 0.f) f = cmake(c.re / m, c.im / m);
+    }
+    out[e] = conj_frame ? cmulc(V[e], f) : cmul(V[e], f);
 }
 
 constexpr int kGT = 64;  // output tile
@@ -163,6 +183,18 @@ extern "C" dpl_status dpl_mlp_features(const float* C, int nslc, int64_t npix, i
     const int64_t tot = npix * (int64_t)(nslc * (nslc - 1) / 2);
     k_mlp_features<<<(unsigned)ceil_div(tot, 256), 256, 0, (cudaStream_t)stream>>>(C, nslc, npix, layout, X);
     return check_launch("k_mlp_features");
+}
+
+extern "C" dpl_status dpl_mlp_frame(const float* C, int nslc, int64_t npix, const float* V, int conj_frame,
+                                    float* out, dpl_stream_t stream) {
+    if (nslc < 1 || nslc > 64 || npix < 0) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_mlp_frame: bad shape");
+    if (npix == 0) return DPL_OK;
+    if (!C || !V || !out) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_mlp_frame: null pointer");
+    const int64_t tot = npix * nslc;
+    k_mlp_frame<<<(unsigned)ceil_div(tot, 256), 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const cfloat*>(C), nslc, npix, reinterpret_cast<const cfloat*>(V), conj_frame,
+        reinterpret_cast<cfloat*>(out));
+    return check_launch("k_mlp_frame");
 }
 
 extern "C" dpl_status dpl_gemm_f32(int M, int N, int K, const float* A, int64_t sai, int64_t sak, const float* B,

@@ -4,7 +4,10 @@ EMI finds the eigenvector of |Gamma|^-1 o C by inverse iteration from a constant
 vector (phase_link/_eigenvalues.py:139-205).  ``WarmStartMLP`` reads a pixel's
 coherence magnitudes (the N(N-1)/2 lower |C_ij|) and proposes the starting vector:
 a fully connected network (ReLU on the hidden layers; 190 -> 256 -> 256 -> 40 at
-N=20) trained on EMI solutions of the plain method.  Every step -- features, forward,
+N=20) trained on EMI solutions of the plain method.  Magnitudes carry no phase, so
+the network's output is expressed in the frame of the pixel's own phases (those of
+C_j0, each SLC's interferogram with SLC 0): the data supply the phases, the network
+the rest.  Every step -- features, forward,
 backward, Adam -- runs in the library's own kernels (``dpl_mlp_features``,
 ``dpl_gemm_f32``, ``dpl_relu_grad``, ``dpl_mse_grad``, ``dpl_colsum``, ``dpl_adam``);
 torch only holds the device buffers.
@@ -29,6 +32,16 @@ __all__ = ["WarmStartMLP", "make_training_set", "process_coherence_warm"]
 
 def _check(st, what):
     _lib.check(st, what)
+
+
+def _frame(C, V, conj_frame):
+    """V (npix, N) complex rotated into (conj_frame=0) or out of (1) the phase frame of C."""
+    torch = D.require_cuda()
+    npix, n = V.shape
+    out = torch.empty_like(V)
+    _check(_lib.load().dpl_mlp_frame(D.ptr(C), int(n), npix, D.ptr(V), int(conj_frame), D.ptr(out),
+                                     D.stream_handle()), "dpl_mlp_frame")
+    return out
 
 
 def _features(C, nslc, layout=1):
@@ -131,10 +144,11 @@ class WarmStartMLP:
         """Network input from coherence matrices: layout 1 = (npix, N, N) complex64."""
         return _features(C, self.nslc, layout)
 
-    def predict(self, C, layout=1):
-        """Starting vectors (npix, N) complex64 for coherence matrices C."""
-        Y = self.forward(self.features(C, layout))[-1]
-        return D.torch().view_as_complex(Y.view(-1, self.nslc, 2).contiguous())
+    def predict(self, C):
+        """Starting vectors (npix, N) complex64 for (npix, N, N) coherence matrices C: the
+        network's output, in the frame of C's phases relative to SLC 0."""
+        Y = self.forward(self.features(C, 1))[-1]
+        return _frame(C, D.torch().view_as_complex(Y.view(-1, self.nslc, 2).contiguous()), 0)
 
     def state(self):
         return {f"W{k}": w.cpu().numpy() for k, w in enumerate(self.W)} | {
@@ -153,7 +167,8 @@ def make_training_set(npix_target, nslc=20, half_window=(5, 11), tile=64, seed=2
     Tiles of ``tile x tile`` output pixels, each from its own seeded stack with
     gamma0 ~ U[0.3, 0.95], gamma_inf ~ U[0, 0.3], tau ~ U[12, 120] days.  Returns
     (X features (npix, nf), T targets (npix, 2N): the unit-norm EMI vector referenced to
-    SLC 0), both float32 on the device.
+    SLC 0 and expressed in the frame of C's phases relative to SLC 0), float32 on the
+    device.
     """
     torch = D.require_cuda()
     from .phase_link import estimate_stack_covariance, process_coherence_matrices
@@ -172,8 +187,9 @@ def make_training_set(npix_target, nslc=20, half_window=(5, 11), tile=64, seed=2
         C = C.contiguous()
         v, _val, est, _crlb = process_coherence_matrices(C, compute_crlb=False)
         keep = (est == 1) & torch.isfinite(torch.view_as_real(v)).all(-1).all(-1)
-        v = v[keep] / math.sqrt(nslc)
-        feats.append(_features(C[keep].contiguous(), nslc))
+        Ck = C[keep].contiguous()
+        v = _frame(Ck, (v[keep] / math.sqrt(nslc)).contiguous(), 1)  # into the frame of C's phases
+        feats.append(_features(Ck, nslc))
         targs.append(torch.view_as_real(v).reshape(v.shape[0], 2 * nslc).contiguous())
         got += int(keep.sum().item())
         k += 1

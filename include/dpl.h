@@ -219,6 +219,12 @@ dpl_status dpl_process_coherence_warm(const float* C, int64_t npix, int nslc, in
 dpl_status dpl_mlp_features(const float* C, int nslc, int64_t npix, int layout, float* X,
                             dpl_stream_t stream);
 
+/* out_j = V_j * f_j (conj_frame: V_j * conj(f_j)) with f_j = exp(i angle C_j0), f_0 = 1:
+ * the network's outputs live in the frame of each pixel's phases relative to SLC 0.
+ * C (npix, nslc, nslc) complex64; V, out (npix, nslc) complex64. */
+dpl_status dpl_mlp_frame(const float* C, int nslc, int64_t npix, const float* V, int conj_frame,
+                         float* out, dpl_stream_t stream);
+
 /* C = act(alpha * op(A) op(B)^T + bias) (+ beta * C), fp32: element (i, k) of op(A) at
  * A[i * sai + k * sak], (j, k) of op(B) at B[j * sbj + k * sbk], C row stride sci; bias
  * per column j or NULL; act = ReLU if relu, else identity.  M x N x K. */
