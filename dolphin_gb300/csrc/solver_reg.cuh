@@ -244,15 +244,14 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     bool crlb_ok = false;
     float dg = 0.f;
     if (!(a.use_evd && !a.compute_crlb)) {
+        // |Gamma| row by a compact loop into shared memory, then into the register slots
+        if (row)
+            for (int j = 0; j < n; ++j) Gi[j] = s_gamma(a, Ci[j], j == me);
         float g[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
             float x = 0.f;
-            if (row && j < n) {
-                x = s_gamma(a, Ci[j], j == me);
-                Gi[j] = x;
-                if (j == me) x = fadd(x, 1e-6f);
-            }
+            if (row && j < n) x = j == me ? fadd(Gi[j], 1e-6f) : Gi[j];
             g[j] = x;
         }
 #pragma unroll 1
@@ -297,8 +296,10 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     cfloat v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
     float lambda;
     int steps = 0;
+    // one matrix slot array and one iteration for both estimators: EMI iterates with
+    // -(A - 0.99 I)^{-1} (the negated sweep result), EVD with C o |C|
+    cfloat mat[K];
     if (!evd) {
-        cfloat am[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
             cfloat x = cmake(0.f, 0.f);
@@ -306,34 +307,43 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
                 x = cscale(Ci[j], Gi[j]);
                 if (j == me) x.re = fsub(x.re, 0.99f);
             }
-            am[j] = x;
+            mat[j] = x;
         }
-        if (!r_sweep_c<K, G>(am, n, cb, gr)) {
+        if (!r_sweep_c<K, G>(mat, n, cb, gr)) {
             if (me == 0) a.fb_list[atomicAdd(a.fb_count, 1)] = (int)p;
             if (next) r_prefetch<G>(Gs, next, n * n, gr);
             gr.sync();
             return;
         }
-        // am = -(A - 0.99 I)^{-1}: x <- (A - 0.99 I)^{-1} v = -(am v)
-        auto inv_op = [&](cfloat x) {
-            const cfloat y = r_matvec<K, G>(am, x, wb, gr);
-            return cmake(-y.re, -y.im);
-        };
-        bool warm = false;
-        if (a.vstart) {
-            // learned starting vector; plain EMI (constant start) if it is unusable or
-            // the iteration from it does not meet the stopping rule
-            const cfloat w0 = row ? a.vstart[p * n + me] : cmake(0.f, 0.f);
-            const float w2 = gr.sum(cabs2(w0));
-            if (w2 > 0.f && w2 <= 3.4e38f) {
-                v = cscale(w0, 1.f / sqrtf(w2));
-                warm = true;
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            cfloat x = cmake(0.f, 0.f);
+            if (row && j < n) {
+                const cfloat c = Ci[j];
+                x = cscale(c, sqrtf(c.re * c.re + c.im * c.im));
             }
+            mat[j] = x;
         }
-        if (!r_iterate<G>(v, gr, steps, inv_op) && warm) {
-            v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
-            r_iterate<G>(v, gr, steps, inv_op);
+    }
+    const float sgn = evd ? 1.f : -1.f;
+    auto op = [&](cfloat x) { return cscale(r_matvec<K, G>(mat, x, wb, gr), sgn); };
+    bool warm = false;
+    if (a.vstart && !evd) {
+        // learned starting vector; plain EMI (constant start) if it is unusable or the
+        // iteration from it does not meet the stopping rule
+        const cfloat w0 = row ? a.vstart[p * n + me] : cmake(0.f, 0.f);
+        const float w2 = gr.sum(cabs2(w0));
+        if (w2 > 0.f && w2 <= 3.4e38f) {
+            v = cscale(w0, 1.f / sqrtf(w2));
+            warm = true;
         }
+    }
+    if (!r_iterate<G>(v, gr, steps, op) && warm) {
+        v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
+        r_iterate<G>(v, gr, steps, op);
+    }
+    if (!evd) {
         // lambda = Re v^H A v, A_ij = |Gamma|^{-1}_ij C_ij
         gr.sync();
         wb[me] = v;
@@ -348,18 +358,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
         v = cscale(v, sqrtf((float)n) / sqrtf(n2));
     } else {
         if (next) r_prefetch<G>(Gs, next, n * n, gr);
-        cfloat h[K];
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-            cfloat x = cmake(0.f, 0.f);
-            if (row && j < n) {
-                const cfloat c = Ci[j];
-                x = cscale(c, sqrtf(c.re * c.re + c.im * c.im));
-            }
-            h[j] = x;
-        }
-        r_iterate<G>(v, gr, steps, [&](cfloat x) { return r_matvec<K, G>(h, x, wb, gr); });
-        const cfloat y = r_matvec<K, G>(h, v, wb, gr);
+        const cfloat y = op(v);
         lambda = gr.sum(v.re * y.re + v.im * y.im);
     }
     // reference to reference_idx
