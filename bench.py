@@ -297,11 +297,35 @@ def run_ours(args, rank, world, pool, cores):
     torch.cuda.empty_cache()
     dstack = torch.empty(host_stack.shape, dtype=host_stack.dtype, device=dev)
 
+    # pipelined: the stack goes up in row bands (each with its halo) on one copy stream,
+    # each block row starts as soon as its band has landed, and its results go down on a
+    # second copy stream while the next block row computes
+    comp = torch.cuda.current_stream()
+    copy_in, copy_out = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    block_rows = sorted({orr for (*_x, orr, _occ) in plan})
+    bands = [(max(0, r0 - HALF[0]), min(frame, r1 + HALF[0])) for (r0, r1) in block_rows]
+
     def e2e_step():
-        dstack.copy_(host_stack, non_blocking=True)
-        gpu_step(dstack, plan, dp, (cpx_full, tc_full))
-        host_cpx.copy_(cpx_full, non_blocking=True)
-        host_tc.copy_(tc_full, non_blocking=True)
+        copy_in.wait_stream(comp)  # the previous step no longer reads dstack
+        landed = []
+        with torch.cuda.stream(copy_in):
+            for (b0, b1) in bands:
+                for t in range(NSLC):  # contiguous (rows, cols) slabs of pinned memory
+                    dstack[t, b0:b1].copy_(host_stack[t, b0:b1], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(copy_in)
+                landed.append(ev)
+        for (r0, r1), ev in zip(block_rows, landed):
+            comp.wait_event(ev)
+            gpu_step(dstack, [e for e in plan if e[4] == (r0, r1)], dp, (cpx_full, tc_full))
+            done = torch.cuda.Event()
+            done.record(comp)
+            with torch.cuda.stream(copy_out):
+                copy_out.wait_event(done)
+                for t in range(NSLC):
+                    host_cpx[t, r0:r1].copy_(cpx_full[t, r0:r1], non_blocking=True)
+                host_tc[r0:r1].copy_(tc_full[r0:r1], non_blocking=True)
+        comp.wait_stream(copy_out)  # the step ends when every result is on the host
 
     e2e_step()
     torch.cuda.synchronize()
@@ -317,7 +341,7 @@ def run_ours(args, rank, world, pool, cores):
     torch.cuda.synchronize()
     barrier()
     e2e_ms = f0.elapsed_time(f1) / e2e_steps
-    h2d = host_stack.numel() * host_stack.element_size()
+    h2d = sum((b1 - b0) for (b0, b1) in bands) * NSLC * frame * host_stack.element_size()
     d2h = host_cpx.numel() * host_cpx.element_size() + host_tc.numel() * host_tc.element_size()
 
     ms, e2e_ms, cov_ms, sol_ms = max_over_ranks([ms, e2e_ms, cov_ms, sol_ms], dist, dev)
