@@ -6,6 +6,8 @@ Public entry points keep the reference's names, arguments and outputs:
 * :func:`estimate_neighbors` (dolphin.shp.estimate_neighbors)
 * :func:`calc_ps_block`      (dolphin.ps.calc_ps_block)
 * :func:`compress`           (dolphin.phase_link.compress)
+* :func:`median_similarity`, :func:`max_similarity`, :func:`get_circle_idxs`
+  (dolphin.similarity)
 
 All compute runs in hand-written CUDA kernels for sm_103a behind the C ABI in
 ``include/dpl.h`` (``dolphin_gb300/_lib/libdpl.so``).  Importing this package
@@ -27,6 +29,7 @@ from .phase_link import (
 )
 from .ps import calc_ps_block
 from .shp import estimate_neighbors
+from .similarity import get_circle_idxs, max_similarity, median_similarity, stack_similarity
 
 __all__ = [
     "EstimatorType",
@@ -40,9 +43,13 @@ __all__ = [
     "compress",
     "estimate_neighbors",
     "estimate_stack_covariance",
+    "get_circle_idxs",
     "install_into_dolphin",
+    "max_similarity",
+    "median_similarity",
     "process_coherence_matrices",
     "run_phase_linking",
+    "stack_similarity",
     "tune_forms",
 ]
 
@@ -58,6 +65,9 @@ _PATCH_TARGETS = (
     ("dolphin.phase_link", "compress"),
     ("dolphin.phase_link._compress", "compress"),
     ("dolphin.workflows.single", "compress"),
+    # similarity.py:300-303 looks median_similarity / max_similarity up at call time
+    ("dolphin.similarity", "median_similarity"),
+    ("dolphin.similarity", "max_similarity"),
 )
 
 
@@ -79,6 +89,8 @@ def install_into_dolphin(modules=None):
         "estimate_neighbors": estimate_neighbors,
         "calc_ps_block": calc_ps_block,
         "compress": compress,
+        "median_similarity": median_similarity,
+        "max_similarity": max_similarity,
     }
     patched = []
 

@@ -69,6 +69,10 @@ SIGNATURES = {
     "dpl_process_coherence_workspace_size": (_sz, [_i64]),
     "dpl_process_coherence": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _sz, _p]),
     "dpl_compress": (_i, [_p, _i64, _i64, _i64, _p, _i64, _i64, _i, _p, _i, _i, _p, _p]),
+    "dpl_circle_offsets": (_i, [_i, _i, _i, _p, _i64, C.POINTER(C.c_int64)]),
+    "dpl_similarity_max_radius": (_i, []),
+    "dpl_similarity_prep": (_i, [_p, _i, _i64, _i64, _i64, _p, _i, _p, _i64, _p, _p]),
+    "dpl_similarity": (_i, [_p, _i64, _i64, _i64, _i, _i, _p, _p]),
     "dpl_process_coherence_warm": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _p,
                                         _p, _sz, _p]),
     "dpl_mlp_features": (_i, [_p, _i, _i64, _i, _p, _p]),

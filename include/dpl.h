@@ -195,6 +195,50 @@ dpl_status dpl_compress(const float* slc, int64_t nslc, int64_t rows, int64_t co
                         int reference_idx, float* comp_slc, dpl_stream_t stream);
 
 /* ---------------------------------------------------------------------------------
+ * Phase-similarity raster (similarity.py).
+ * ------------------------------------------------------------------------------- */
+
+/* Replaces: get_circle_idxs(max_radius, min_radius, sort_output) -- similarity.py:176-254.
+ * Host-only (no device work).  Writes up to `capacity` (row, col) pairs to `offsets`
+ * ((capacity, 2) int32, may be NULL) and the number of offsets to `count`, in the
+ * reference's order (ring by ring), or sorted lexicographically if sort_output != 0.
+ * max_radius < 1 is an error (the reference raises). */
+dpl_status dpl_circle_offsets(int max_radius, int min_radius, int sort_output, int32_t* offsets,
+                              int64_t capacity, int64_t* count);
+
+/* Largest search_radius dpl_similarity accepts (11: every radius the reference's
+ * workflows use, 7 and 11). */
+int dpl_similarity_max_radius(void);
+
+/* Replaces the preparation in _create_loop_and_run -- similarity.py:96-117 -- and, with
+ * nearest_n > 0, _calc_nearest_diffs / _create_nearest_n_pairs -- similarity.py:355-375
+ * (pairs (i, j), i < j <= i + nearest_n, of the nlayers + 1 dates of a single-reference
+ * stack; timeseries.get_incidence_matrix, timeseries.py:594-644).
+ * stack       : (nlayers, rows, cols) complex64 (is_complex != 0) or float32 phase
+ * mask        : (rows, cols) uint8 or NULL (all pixels)
+ * unit        : (unit_layers, rows, cols) complex64 out -- exp(i angle z), exp(i phase) or
+ *               exp(i (phi_j - phi_i)); NaN on pixels that are not valid.  unit_layers
+ *               must be nlayers, or the number of nearest-n pairs.
+ * valid       : (rows, cols) uint8 out -- mask and not invalid, where invalid means the
+ *               layer-by-layer float32 sum of nan_to_num(z) is exactly 0 (with
+ *               nearest_n > 0 also: some layer's phase is not finite, which makes every
+ *               pair NaN in the reference's matrix product). */
+dpl_status dpl_similarity_prep(const float* stack, int is_complex, int64_t nlayers, int64_t rows,
+                               int64_t cols, const uint8_t* mask, int nearest_n, float* unit,
+                               int64_t unit_layers, uint8_t* valid, dpl_stream_t stream);
+
+/* Replaces: median_similarity / max_similarity(ifg_stack, search_radius, mask) --
+ * similarity.py:31-93, loop _make_loop_function, similarity.py:120-173.
+ * unit  : (nlayers, rows, cols) complex64 from dpl_similarity_prep
+ * kind  : 0 median (nanmedian), 1 max (nanmax) of the similarities
+ *         mean_t Re(u_t(p) conj u_t(q)) over the circle's neighbours q of p, each
+ *         coordinate clipped to the image, p itself and NaN similarities left out
+ * out   : (rows, cols) float32 out; NaN where no similarity is left.
+ * 1 <= search_radius <= dpl_similarity_max_radius(). */
+dpl_status dpl_similarity(const float* unit, int64_t nlayers, int64_t rows, int64_t cols,
+                          int search_radius, int kind, float* out, dpl_stream_t stream);
+
+/* ---------------------------------------------------------------------------------
  * Learned EMI warm start (no counterpart in the reference, whose EMI inverse iteration
  * starts from a constant vector, phase_link/_eigenvalues.py:139-205).
  * ------------------------------------------------------------------------------- */

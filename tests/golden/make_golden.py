@@ -276,10 +276,74 @@ def make_compress():
     _save("compress", ncases=np.array(len(cases)), **out)
 
 
+def make_similarity():
+    """similarity.py: circle offsets, phase_similarity, median/max rasters (masks, NaNs,
+    zeros, real phase input, clipping at the edges) and the nearest-n differences."""
+    S = R.similarity
+    out = {}
+    for radius in range(1, 26):
+        out[f"circle_{radius}"] = np.asarray(S.get_circle_idxs(radius)).reshape(-1, 2).astype(np.int16)
+    for radius, rmin in [(5, 0), (7, 2), (9, 4)]:
+        out[f"circle_raw_{radius}_{rmin}"] = np.asarray(
+            S.get_circle_idxs(radius, min_radius=rmin, sort_output=False)).reshape(-1, 2).astype(np.int16)
+    # phase_similarity on the reference's known-answer vectors and a random pair
+    rng = np.random.default_rng(801)
+    x1 = np.exp(1j * rng.uniform(0, 2 * np.pi, 50)).astype(np.complex64)
+    x2 = np.exp(1j * rng.uniform(0, 2 * np.pi, 50)).astype(np.complex64)
+    out["ps_x1"], out["ps_x2"] = x1, x2
+    out["ps_val"] = np.array([S.phase_similarity(x1, x2), S.phase_similarity(x1, x1),
+                              S.phase_similarity(np.zeros(10, np.complex64), np.zeros(10, np.complex64))])
+
+    def ifgs(seed, n, rows, cols):
+        z = make_stack(StackConfig(nslc=n + 1, rows=rows, cols=cols, seed=seed, ps_frac=0.0))
+        return (z[1:] * np.conj(z[:1])).astype(np.complex64)
+
+    cases = []
+    a = ifgs(802, 8, 13, 17)
+    a[:, 2, 3] = np.nan  # a pixel with no data
+    a[:, 5, 0] = 0  # an all-zero pixel (invalid)
+    a[3, 7, 9] = np.nan  # one NaN layer: its similarities are NaN
+    cases += [("cpx", a, r, None) for r in (2, 3, 5)]
+    b = ifgs(803, 6, 5, 10)
+    mask = np.array(
+        [[1, 0, 0, 1, 0, 0, 0, 0, 1, 1], [0, 1, 1, 1, 1, 1, 1, 1, 0, 1], [1, 0, 0, 0, 0, 1, 1, 0, 1, 0],
+         [1, 1, 1, 1, 1, 0, 1, 0, 0, 0], [0, 0, 1, 1, 1, 1, 1, 1, 0, 1]], dtype=bool)
+    cases += [("masked", b, r, mask) for r in (2, 5, 9)]
+    ph = np.angle(ifgs(804, 5, 9, 11)).astype(np.float32)
+    ph[:, 4, 4] = 0.0  # zero phase everywhere: invalid
+    cases += [("real", ph, 4, None)]
+    cases += [("row", ifgs(805, 4, 1, 12), 3, None), ("col", ifgs(806, 4, 11, 1), 3, None)]
+    cases += [("zeros", np.zeros((10, 4, 5), np.complex64), 2, None),
+              ("nans", np.full((10, 4, 5), np.nan, np.complex64), 2, None)]
+    for k, (name, stack, radius, m) in enumerate(cases):
+        m_med = None if m is None else m.copy()
+        m_max = None if m is None else m.copy()
+        med = S.median_similarity(stack.copy(), search_radius=radius, mask=m_med)
+        mx = S.max_similarity(stack.copy(), search_radius=radius, mask=m_max)
+        out[f"case_{k}_stack"], out[f"case_{k}_radius"] = stack, np.array(radius)
+        out[f"case_{k}_median"], out[f"case_{k}_max"] = np.asarray(med), np.asarray(mx)
+        if m is not None:
+            out[f"case_{k}_mask_in"], out[f"case_{k}_mask_after"] = m, m_med
+        print(f"  similarity case {k} ({name}, radius {radius})")
+    out["ncases"] = np.array(len(cases))
+    # nearest-n differences of a single-reference stack (3 nearest dates, 7 + 1 dates)
+    c = ifgs(807, 7, 10, 12)
+    c[:, 1, 1] = np.nan
+    c[2, 3, 4] = np.nan
+    c[:, 6, 6] = 0
+    pairs = S._create_nearest_n_pairs(c.shape[0] + 1, n=3)
+    A = R.get_incidence_matrix(pairs)
+    d = S._calc_nearest_diffs(c.copy(), A)
+    out["nn_stack"], out["nn_pairs"], out["nn_diffs"] = c, np.array(pairs), np.asarray(d)
+    out["nn_median"] = np.asarray(S.median_similarity(d.copy(), search_radius=3))
+    _save("similarity", **out)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["ps", "glrt", "ks", "covariance", "phase_link", "config1", "ps_fill", "compress"]
+    which = sys.argv[1:] or ["ps", "glrt", "ks", "covariance", "phase_link", "config1", "ps_fill", "compress",
+                             "similarity"]
     for w in which:
         print(f"[{w}]")
         {"ps": make_ps, "glrt": make_glrt, "ks": make_ks, "covariance": make_covariance,
          "phase_link": make_phase_link, "config1": make_config1_crop, "ps_fill": make_ps_fill,
-         "compress": make_compress}[w]()
+         "compress": make_compress, "similarity": make_similarity}[w]()

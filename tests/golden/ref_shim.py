@@ -346,6 +346,22 @@ def _package(modname, path):
     return pkg
 
 
+def load_function(path, name, **names):
+    """One top-level function of a reference source file, run from its own source text
+    with ``numpy`` and ``names`` as its globals (for modules whose imports are out of
+    reach here, such as ``timeseries.py``)."""
+    import ast
+
+    text = Path(path).read_text()
+    for node in ast.parse(text).body:
+        if isinstance(node, ast.FunctionDef) and node.name == name:
+            ns = {"np": np, "annotations": None, **names}
+            code = "from __future__ import annotations\n" + ast.get_source_segment(text, node)
+            exec(compile(code, str(path), "exec"), ns)
+            return ns[name]
+    raise KeyError(f"{name} not found in {path}")
+
+
 _LOADED = None
 
 
@@ -396,6 +412,8 @@ def load_reference():
     shp_init = _load_file("dolphin.shp.__init__", REF_SRC / "shp" / "__init__.py")
 
     ps = _load_file("dolphin.ps", REF_SRC / "ps.py")
+    similarity = _load_file("dolphin.similarity", REF_SRC / "similarity.py")
+    incidence = load_function(REF_SRC / "timeseries.py", "get_incidence_matrix", flatten=utils.flatten)
 
     _LOADED = types.SimpleNamespace(
         types=types_mod,
@@ -412,6 +430,8 @@ def load_reference():
         ks=ks,
         shp=shp_init,
         ps=ps,
+        similarity=similarity,
+        get_incidence_matrix=incidence,
         ShpMethod=enums.ShpMethod,
     )
     return _LOADED
