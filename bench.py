@@ -505,6 +505,106 @@ def run_batch(args):
     }), flush=True)
 
 
+SIM_LAYERS, SIM_RADIUS, SIM_SEED = 30, 7, 20261209
+
+
+def run_similarity(args):
+    """Phase-similarity raster (similarity.py create_similarities' block computation,
+    median, search radius 7) of a 30-interferogram single-reference stack, frame x frame."""
+    import torch
+
+    from dolphin_gb300 import _device as D
+    from dolphin_gb300 import _lib
+    from dolphin_gb300._build import build_library
+    from dolphin_gb300.simulate import StackConfig, make_stack_torch
+
+    build_library()
+    lib = _lib.load()
+    frame, m, radius = args.frame, SIM_LAYERS, SIM_RADIUS
+    z = make_stack_torch(StackConfig(nslc=m + 1, rows=frame, cols=frame, seed=SIM_SEED, ps_frac=0.03))
+    ifg = (z[1:] * z[:1].conj()).contiguous()
+    del z
+    unit = torch.empty_like(ifg)
+    valid = torch.empty((frame, frame), dtype=torch.uint8, device="cuda")
+    out = torch.empty((frame, frame), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sh = D.stream_handle()
+
+    def step(src):
+        _lib.check(lib.dpl_similarity_prep(src.data_ptr(), 1, m, frame, frame, None, 0, unit.data_ptr(), m,
+                                           valid.data_ptr(), sh), "dpl_similarity_prep")
+        _lib.check(lib.dpl_similarity(unit.data_ptr(), m, frame, frame, radius, 0, out.data_ptr(), sh),
+                   "dpl_similarity")
+
+    timing = {}
+
+    def timed(fn, steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        for _ in range(steps):
+            fn()
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]) / steps
+
+    for _ in range(max(3, args.warmup)):
+        step(ifg)
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    ms = timed(lambda: step(ifg), args.steps)
+    # the similarity kernel alone, on the phasors just written
+    sim_ms = timed(lambda: _lib.check(lib.dpl_similarity(unit.data_ptr(), m, frame, frame, radius, 0,
+                                                         out.data_ptr(), sh)), args.steps)
+    clocks = sampler.stop()
+    # end to end: pinned host stack in, host raster out
+    host = torch.empty(ifg.shape, dtype=ifg.dtype, pin_memory=True)
+    host.copy_(ifg)
+    host_out = torch.empty((frame, frame), dtype=torch.float32, pin_memory=True)
+    dev_in = torch.empty_like(ifg)
+
+    def e2e():
+        dev_in.copy_(host, non_blocking=True)
+        step(dev_in)
+        host_out.copy_(out, non_blocking=True)
+
+    e2e()
+    e2e_ms = timed(e2e, args.steps)
+    px = frame * frame
+    # algorithmic work: K circle offsets x m layers x 4 flops (Re(x conj y)) per pixel
+    from dolphin_gb300.similarity import get_circle_idxs
+
+    K = len(get_circle_idxs(radius))
+    flops = px * K * m * 4.0
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 FMA rate, TFLOP/s
+    line = {
+        "workload": "similarity", "metric": f"phase-similarity pixels/sec (median, radius {radius}, {m} layers)",
+        "value": px / (ms / 1000.0), "unit": UNIT, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{m} single-reference interferograms, {frame}x{frame}, median similarity, "
+                               f"search radius {radius} ({K} neighbours)", "l2": f"inputs larger than L2 "
+                               f"({ifg.numel() * 8 / 1e9:.1f} GB)"},
+        "e2e": {"value": px / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": ifg.numel() * 8,
+                "d2h_bytes_per_step": px * 4},
+        "roofline": {"bound": "fp32", "kernel": "k_similarity", "kernel_ms": sim_ms,
+                     "achieved": flops / (sim_ms / 1000.0) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": flops / (sim_ms / 1000.0) / 1e12 / fp32_peak,
+                     "note": "algorithmic flops K*m*4 per pixel over the CUDA-event kernel time; peak = nominal "
+                             "FP32 FMA rate (no measured FP32 peak on this pool)"},
+        "clocks": clocks,
+    }
+    if not args.no_cpu:
+        from oracle import similarity as O
+
+        crop = ifg[:, :256, :256].cpu().numpy()
+        t0 = time.perf_counter()
+        O.median_similarity(crop, radius)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": crop.shape[1] * crop.shape[2] / dt, "unit": UNIT, "cores": 1,
+                                "kind": "port", "sample": "numpy restatement on a 256x256 crop, 1 process"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -513,10 +613,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frame", type=int, default=FRAME)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--workload", default="config2", choices=["config2", "precision", "batch"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "precision", "batch", "similarity"],
                     help="precision: N=40 2048x2048 stack, half-window (7, 7), low gamma_inf with a "
                          "high-coherence disk; rates of the tensor-core and SIMT covariance forms. "
-                         "batch: 12 ministacks of N = 8..45, 1024x1024 each, as one CUDA graph")
+                         "batch: 12 ministacks of N = 8..45, 1024x1024 each, as one CUDA graph. "
+                         "similarity: median phase similarity, radius 7, of 30 interferograms")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -528,6 +629,9 @@ def main():
         return
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "similarity":
+        run_similarity(args)
         return
     pool = None
     cores = len(os.sched_getaffinity(0))

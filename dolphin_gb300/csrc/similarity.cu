@@ -20,9 +20,9 @@
 //                neighbours in that column (each load serves P pixels).  The circle's
 //                K similarities of a pixel thus sit in the registers of its group, and
 //                the summary is taken there: the maximum by a group reduction, the
-//                median by a radix selection on order-preserving keys with one
-//                group-wide count per bit (redux.sync), from the highest bit in which
-//                the group's smallest and largest key differ.  The pixel itself (which
+//                median by a selection on order-preserving keys, each step one
+//                group-wide count (redux.sync) around an interpolated pivot.  The
+//                pixel itself (which
 //                a clipped offset reaches at the image edge) and NaN similarities are
 //                left out.
 #include <algorithm>
@@ -216,7 +216,6 @@ __global__ void __launch_bounds__(256) k_sim_prep(SimPrepArgs a) {
 // ----------------------------------------------------------------------------------
 // similarity
 // ----------------------------------------------------------------------------------
-constexpr int kSimThreads = 512;
 constexpr int kSimChunk = 8;  // layers per staged chunk
 
 struct SimArgs {
@@ -230,14 +229,17 @@ struct SimArgs {
 
 // Work layout for largest offset H.  A group of G lanes (G >= 2H + 1) owns P vertically
 // adjacent pixels of one column; its lane dc + H accumulates their similarities with
-// the 2H + 1 neighbours in column c + dc.  A CTA of 512 threads owns TC x TR pixels.
+// the 2H + 1 neighbours in column c + dc.  A CTA owns TC x TR pixels.
 template <int H>
 struct SimShape {
     static constexpr int D = 2 * H + 1;
     static constexpr int G = D <= 4 ? 4 : D <= 8 ? 8 : D <= 16 ? 16 : 32;
     static constexpr int P = H <= 10 ? 4 : 2;
     static constexpr int GPW = 32 / G;
-    static constexpr int UNITS = kSimThreads / 32 * GPW;
+    // 256 threads (two CTAs per SM, which drift apart so that one accumulates while the
+    // other takes its summaries) except for the widest groups, whose tiles would be thin
+    static constexpr int THREADS = G == 32 ? 512 : 256;
+    static constexpr int UNITS = THREADS / 32 * GPW;
     static constexpr int TC = G == 4 ? 32 : 16;
     static constexpr int TR = UNITS / TC * P;
     static constexpr int TRH = TR + 2 * H, SW = TC + 2 * H;  // staged rows and columns
@@ -262,43 +264,90 @@ __device__ __forceinline__ float sim_unkey(uint32_t k) {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// k-th smallest (0-based) of the n keys that the group holds (key[i] of every lane where
-// bit i of vm is set; all in [lo, hi]): radix selection from the highest bit in which lo
-// and hi differ, one group-wide count per bit, stopping as soon as one key is left.
+// Reductions over the G-lane groups of a warp, executed by all 32 lanes together so
+// that no collective runs under divergence: sums through one warp-wide redux of
+// per-group bit fields (a group's sum never exceeds its field), minima and maxima
+// through xor butterflies that stay inside each group.
+template <int G>
+struct SimGroup {
+    static constexpr int FW = G;  // bits of a group's field: 32 / (32 / G)
+    int shift;
+    __device__ __forceinline__ explicit SimGroup(int lane) : shift((lane / G) * G) {}
+    __device__ __forceinline__ int sum(int v) const {
+        const unsigned t = __reduce_add_sync(0xffffffffu, (unsigned)v << shift);
+        if (FW == 32) return (int)t;
+        return (int)((t >> shift) & ((1u << (FW & 31)) - 1u));
+    }
+    __device__ __forceinline__ uint32_t min(uint32_t v) const {
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) v = ::min(v, __shfl_xor_sync(0xffffffffu, v, o));
+        return v;
+    }
+    __device__ __forceinline__ uint32_t max(uint32_t v) const {
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) v = ::max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        return v;
+    }
+};
+
+// Number of keys below t, summed as a tree (no long chain of dependent adds).
 template <int D>
-__device__ __forceinline__ uint32_t sim_kth(const uint32_t (&key)[D], uint32_t vm, unsigned gmask, uint32_t lo,
-                                            uint32_t hi, int n, int k) {
-    if (lo == hi) return lo;
-    int b = 31 - __clz(lo ^ hi);
-    uint32_t prefix = lo & ~(0xffffffffu >> (31 - b));
-    int cand = n;
-    for (; b >= 0; --b) {
-        const uint32_t want = prefix >> b;  // bit b of the prefix is 0
-        int c0 = 0;
+__device__ __forceinline__ int sim_count_below(const uint32_t (&key)[D], uint32_t t) {
+    int part[4] = {0, 0, 0, 0};
 #pragma unroll
-        for (int i = 0; i < D; ++i) c0 += (((vm >> i) & 1u) && (key[i] >> b) == want) ? 1 : 0;
-        c0 = (int)__reduce_add_sync(gmask, (unsigned)c0);
-        if (k < c0) {
-            cand = c0;
+    for (int i = 0; i < D; ++i) part[i & 3] += key[i] < t ? 1 : 0;
+    return (part[0] + part[1]) + (part[2] + part[3]);
+}
+
+// Key of rank k (0-based, among the group's n valid keys; a left-out entry has key 0,
+// below every key of a number, and a lane holds `zeros` of them) given that it lies in
+// [L, U], `below` valid keys are < L and `upto` are <= U.  Each step counts the valid
+// keys below a pivot t with one group-wide reduction and keeps the side that holds rank
+// k.  The pivot interpolates the rank linearly in value between L and U (a pixel's
+// similarities are spread fairly evenly; about 7 steps for a median of 20 to 140), or
+// bisects [L, U] in key order after a step that did not halve it, so the key range at
+// least halves every two steps (at most 64 steps).  The warp steps until all its groups
+// are done.
+template <int D, int G>
+__device__ __forceinline__ uint32_t sim_kth(const uint32_t (&key)[D], int zeros, const SimGroup<G>& grp, uint32_t L,
+                                            uint32_t U, int below, int upto, int k) {
+    bool bisect = false;
+    for (int it = 0; it < 80; ++it) {
+        const bool live = L < U && upto - below > 1;
+        if (!__any_sync(0xffffffffu, live)) break;
+        uint32_t t;
+        if (bisect) {
+            t = L + ((U - L) >> 1) + 1u;
         } else {
-            k -= c0;
-            prefix |= 1u << b;
-            cand -= c0;
+            const float lv = sim_unkey(L), uv = sim_unkey(U);
+            const float f = ((float)(k - below) + 0.5f) / (float)max(upto - below, 1);
+            t = min(max(sim_key(fmaf(uv - lv, f, lv)), L + 1u), U);
         }
-        if (cand == 1) {
-            const uint32_t w = prefix >> b;
-            uint32_t f = 0;
-#pragma unroll
-            for (int i = 0; i < D; ++i)
-                if (((vm >> i) & 1u) && (key[i] >> b) == w) f = key[i];
-            return __reduce_max_sync(gmask, f);
+        const int c_lane = sim_count_below<D>(key, t) - zeros;
+        const int c = grp.sum(live ? c_lane : 0);  // valid keys < t (a finished group adds nothing: its
+                                    // pivot need not exceed its zeros)
+        if (live) {
+            const uint32_t span = U - L;
+            if (k < c) {
+                U = t - 1u;
+                upto = c;
+            } else {
+                L = t;
+                below = c;
+            }
+            bisect = !bisect && U - L > span / 2;
         }
     }
-    return prefix;
+    uint32_t f = 0;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        if (key[i] >= L && key[i] <= U) f = ::max(f, key[i]);
+    f = grp.max(f);
+    return L == U ? L : f;
 }
 
 template <int H>
-__global__ void __launch_bounds__(kSimThreads, 1) k_similarity(SimArgs a) {
+__global__ void __launch_bounds__(SimShape<H>::THREADS, 512 / SimShape<H>::THREADS) k_similarity(SimArgs a) {
     using S = SimShape<H>;
     constexpr int D = S::D, G = S::G, P = S::P;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -311,25 +360,32 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_similarity(SimArgs a) {
     const int lc = active ? gl : D - 1;  // idle lanes read an in-bounds column
     const int dc = gl - H;
     const int hc = active ? a.hc[gl] : -1;
-    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane / G * G));
+    uint32_t run = 0;  // bit i: row offset i - H belongs to this lane's column of the circle
+#pragma unroll
+    for (int i = 0; i < 2 * H + 1; ++i)
+        if (i - H >= -hc && i - H <= hc && !(dc == 0 && i == H)) run |= 1u << i;
     const int64_t npix = (int64_t)a.rows * a.cols;
     const int nch = (a.m + kSimChunk - 1) / kSimChunk;
     const int my_tiles = a.tiles > (int)blockIdx.x ? (a.tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const int steps = my_tiles * nch;
 
+    // one warp copies whole staged rows, a lane per column: the clipped source column is
+    // per lane, the clipped source row per warp
     auto issue = [&](int s) {
         const int tile = blockIdx.x + (s / nch) * gridDim.x, ch = s % nch;
         const int r0 = (tile / a.tiles_c) * S::TR, c0 = (tile % a.tiles_c) * S::TC;
         float2* dst = stages + (s & 1) * S::STAGE;
-        for (int e = threadIdx.x; e < S::STAGE; e += kSimThreads) {
-            const int j = e / S::LAYER, rem = e - j * S::LAYER;
-            const int tr = rem / S::SW, tc = rem - tr * S::SW;
+        const int ca = min(max(c0 - H + lane, 0), a.cols - 1);
+        const int cb = min(max(c0 - H + lane + 32, 0), a.cols - 1);
+        for (int row = warp; row < kSimChunk * S::TRH; row += S::THREADS / 32) {
+            const int j = row / S::TRH, tr = row - j * S::TRH;
             const int layer = ch * kSimChunk + j;
-            const int r = min(max(r0 - H + tr, 0), a.rows - 1);
-            const int c = min(max(c0 - H + tc, 0), a.cols - 1);
             const bool inside = layer < a.m;
-            const float2* src = a.unit + (inside ? (int64_t)layer * npix + (int64_t)r * a.cols + c : 0);
-            sim_cp8(dst + e, src, inside);
+            const int r = min(max(r0 - H + tr, 0), a.rows - 1);
+            const float2* src = a.unit + (inside ? (int64_t)layer * npix + (int64_t)r * a.cols : 0);
+            float2* d = dst + row * S::SW;
+            if (lane < S::SW) sim_cp8(d + lane, src + (inside ? ca : 0), inside);
+            if (S::SW > 32 && lane + 32 < S::SW) sim_cp8(d + lane + 32, src + (inside ? cb : 0), inside);
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
@@ -351,82 +407,86 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_similarity(SimArgs a) {
         const int ch = s % nch;
         const float2* T = stages + (s & 1) * S::STAGE;
         const int nl = min(kSimChunk, a.m - ch * kSimChunk);
-#pragma unroll 1
+        constexpr int kUnroll = H <= 7 ? 2 : 1;  // two layers in flight where registers allow
+#pragma unroll(kUnroll)
         for (int j = 0; j < nl; ++j) {
             const float2* colp = T + j * S::LAYER + (rb * P) * S::SW + cu + lc;
             const float2* ownp = T + j * S::LAYER + (rb * P + H) * S::SW + cu + H;
-            float2 own[P];
+            float2 own[P], v[D + P - 1];
 #pragma unroll
             for (int p = 0; p < P; ++p) own[p] = ownp[p * S::SW];
 #pragma unroll
-            for (int t = 0; t < D + P - 1; ++t) {
-                const float2 v = colp[t * S::SW];
+            for (int t = 0; t < D + P - 1; ++t) v[t] = colp[t * S::SW];
+            // all real-part products first, then the imaginary ones: the two multiply-adds
+            // of an accumulator are far apart in the instruction stream
 #pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    const int i = t - p;
-                    if (i >= 0 && i < D) acc[p][i] = fmaf(own[p].y, v.y, fmaf(own[p].x, v.x, acc[p][i]));
-                }
-            }
+            for (int t = 0; t < D + P - 1; ++t)
+#pragma unroll
+                for (int p = 0; p < P; ++p)
+                    if (t - p >= 0 && t - p < D) acc[p][t - p] = fmaf(own[p].x, v[t].x, acc[p][t - p]);
+#pragma unroll
+            for (int t = 0; t < D + P - 1; ++t)
+#pragma unroll
+                for (int p = 0; p < P; ++p)
+                    if (t - p >= 0 && t - p < D) acc[p][t - p] = fmaf(own[p].y, v[t].y, acc[p][t - p]);
         }
         if (ch == nch - 1) {
-            // the tile's sums are complete: summaries of the group's P pixels
+            // the tile's sums are complete: summaries of the group's P pixels, all lanes
+            // of the warp in step
             const int tile = blockIdx.x + (s / nch) * gridDim.x;
             const int r0 = (tile / a.tiles_c) * S::TR, c = (tile % a.tiles_c) * S::TC + cu;
             const float fm = (float)a.m;
             const bool col_self = dc == 0 || (dc < 0 && c == 0) || (dc > 0 && c == a.cols - 1);
+            const SimGroup<G> grp(lane);
 #pragma unroll
             for (int p = 0; p < P; ++p) {
                 const int r = r0 + rb * P + p;
-                if (r < a.rows && c < a.cols) {  // uniform over the group
-                    uint32_t key[D];
-                    uint32_t vm = 0, kmin = 0xffffffffu, kmax = 0;
-                    int cnt = 0;
-#pragma unroll
-                    for (int i = 0; i < D; ++i) {
-                        const int dr = i - H;
-                        const bool row_self = dr == 0 || (dr < 0 && r == 0) || (dr > 0 && r == a.rows - 1);
-                        const bool use = dr >= -hc && dr <= hc && !(dc == 0 && dr == 0) && !(row_self && col_self) &&
-                                         !isnan(acc[p][i]);
-                        key[i] = sim_key(acc[p][i]);
-                        if (use) {
-                            vm |= 1u << i;
-                            ++cnt;
-                            kmin = min(kmin, key[i]);
-                            kmax = max(kmax, key[i]);
-                        }
-                    }
-                    const int n = (int)__reduce_add_sync(gmask, (unsigned)cnt);
-                    float res = __int_as_float(0x7fffffff);
-                    if (n > 0) {
-                        const uint32_t gmax = __reduce_max_sync(gmask, kmax);
-                        if (a.kind == 1) {
-                            res = sim_unkey(gmax) / fm;
-                        } else {
-                            const uint32_t gmin = __reduce_min_sync(gmask, kmin);
-                            const int k = (n - 1) / 2;  // the median, or the lower one for even n
-                            const uint32_t lo = sim_kth<D>(key, vm, gmask, gmin, gmax, n, k);
-                            res = sim_unkey(lo) / fm;
-                            if (!(n & 1)) {
-                                // upper median: lo again if more than k + 1 keys are <= lo,
-                                // else the smallest key above lo
-                                int le = 0;
-                                uint32_t gt = 0xffffffffu;
-#pragma unroll
-                                for (int i = 0; i < D; ++i) {
-                                    if ((vm >> i) & 1u) {
-                                        le += key[i] <= lo ? 1 : 0;
-                                        if (key[i] > lo) gt = min(gt, key[i]);
-                                    }
-                                }
-                                le = (int)__reduce_add_sync(gmask, (unsigned)le);
-                                gt = __reduce_min_sync(gmask, gt);
-                                const float up = sim_unkey(le >= k + 2 ? lo : gt) / fm;
-                                res = (float)(((double)res + (double)up) * 0.5);
-                            }
-                        }
-                    }
-                    if (gl == 0) a.out[(int64_t)r * a.cols + c] = res;
+                const bool inside = r < a.rows && c < a.cols;
+                // the pixel itself, reached through a clipped offset at the image edge
+                uint32_t self = 0;
+                if (col_self) {
+                    self = 1u << H;
+                    if (r == 0) self |= (1u << H) - 1u;
+                    if (r == a.rows - 1) self |= ((1u << D) - 1u) & ~((2u << H) - 1u);
                 }
+                const uint32_t vm = inside ? run & ~self : 0u;
+                uint32_t key[D];  // 0: left out
+                uint32_t kmin = 0xffffffffu, kmax = 0;
+                int cnt = 0;
+#pragma unroll
+                for (int i = 0; i < D; ++i) {
+                    const bool use = ((vm >> i) & 1u) && !isnan(acc[p][i]);
+                    key[i] = use ? sim_key(acc[p][i]) : 0u;
+                    cnt += use ? 1 : 0;
+                    kmin = ::min(kmin, use ? key[i] : 0xffffffffu);
+                    kmax = ::max(kmax, key[i]);
+                }
+                const int n = grp.sum(cnt);
+                const uint32_t gmax = grp.max(kmax);
+                float res = __int_as_float(0x7fffffff);
+                if (a.kind == 1) {
+                    if (n > 0) res = sim_unkey(gmax) / fm;
+                } else {
+                    const uint32_t gmin = grp.min(kmin);
+                    const int k = n > 0 ? (n - 1) / 2 : 0;  // the median, or the lower one for even n
+                    const uint32_t lo = sim_kth<D, G>(key, D - cnt, grp, gmin, gmax, 0, n, k);
+                    // upper median: lo again if more than k + 1 keys are <= lo, else the
+                    // smallest key above lo
+                    int le = sim_count_below<D>(key, lo + 1u) + cnt - D;
+                    uint32_t gt = 0xffffffffu;
+#pragma unroll
+                    for (int i = 0; i < D; ++i) gt = ::min(gt, key[i] > lo ? key[i] : 0xffffffffu);
+                    le = grp.sum(le);
+                    gt = grp.min(gt);
+                    if (n > 0) {
+                        res = sim_unkey(lo) / fm;
+                        if (!(n & 1)) {
+                            const float up = sim_unkey(le >= k + 2 ? lo : gt) / fm;
+                            res = (float)(((double)res + (double)up) * 0.5);
+                        }
+                    }
+                }
+                if (gl == 0 && inside) a.out[(int64_t)r * a.cols + c] = res;
 #pragma unroll
                 for (int i = 0; i < D; ++i) acc[p][i] = 0.f;  // next tile
             }
@@ -446,10 +506,10 @@ static dpl_status sim_dispatch_h(SimArgs& a, cudaStream_t st) {
     int dev = 0, sms = 0, per_sm = 0;
     DPL_CUDA_TRY(cudaGetDevice(&dev));
     DPL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_similarity<H>, kSimThreads, S::SMEM));
+    DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_similarity<H>, S::THREADS, S::SMEM));
     if (per_sm < 1) return fail(DPL_ERR_UNSUPPORTED, "dpl_similarity: kernel does not fit on an SM");
     const int grid = (int)std::min<int64_t>(tiles, (int64_t)sms * per_sm);
-    k_similarity<H><<<grid, kSimThreads, S::SMEM, st>>>(a);
+    k_similarity<H><<<grid, S::THREADS, S::SMEM, st>>>(a);
     return check_launch("k_similarity");
 }
 
