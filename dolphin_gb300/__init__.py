@@ -8,6 +8,8 @@ Public entry points keep the reference's names, arguments and outputs:
 * :func:`compress`           (dolphin.phase_link.compress)
 * :func:`median_similarity`, :func:`max_similarity`, :func:`get_circle_idxs`
   (dolphin.similarity)
+* :func:`run_wrapped_phase_single`, :func:`run_wrapped_phase_sequential` (the block
+  loop of dolphin.workflows.single / .sequential on device arrays, without raster I/O)
 
 All compute runs in hand-written CUDA kernels for sm_103a behind the C ABI in
 ``include/dpl.h`` (``dolphin_gb300/_lib/libdpl.so``).  Importing this package
@@ -30,6 +32,13 @@ from .phase_link import (
 from .ps import calc_ps_block
 from .shp import estimate_neighbors
 from .similarity import get_circle_idxs, max_similarity, median_similarity, stack_similarity
+from .workflow import (
+    StridedBlockManager,
+    grow_nodata_region,
+    plan_ministacks,
+    run_wrapped_phase_sequential,
+    run_wrapped_phase_single,
+)
 
 __all__ = [
     "EstimatorType",
@@ -39,16 +48,21 @@ __all__ = [
     "PhaseLinkRuntimeError",
     "ShpMethod",
     "Strides",
+    "StridedBlockManager",
     "calc_ps_block",
     "compress",
     "estimate_neighbors",
     "estimate_stack_covariance",
     "get_circle_idxs",
+    "grow_nodata_region",
     "install_into_dolphin",
     "max_similarity",
     "median_similarity",
+    "plan_ministacks",
     "process_coherence_matrices",
     "run_phase_linking",
+    "run_wrapped_phase_sequential",
+    "run_wrapped_phase_single",
     "stack_similarity",
     "tune_forms",
 ]

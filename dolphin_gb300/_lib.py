@@ -73,6 +73,7 @@ SIGNATURES = {
     "dpl_similarity_max_radius": (_i, []),
     "dpl_similarity_prep": (_i, [_p, _i, _i64, _i64, _i64, _p, _i, _p, _i64, _p, _p]),
     "dpl_similarity": (_i, [_p, _i64, _i64, _i64, _i, _i, _p, _p]),
+    "dpl_grow_nodata_region": (_i, [_p, _p, _i, _i64, _i64, _d, _i, _i, _p]),
     "dpl_process_coherence_warm": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p, _p,
                                         _p, _sz, _p]),
     "dpl_mlp_features": (_i, [_p, _i, _i64, _i, _p, _p]),

@@ -34,6 +34,16 @@ typedef enum dpl_status {
     DPL_ERR_TIMEOUT = 6           /* a bounded device-side wait gave up; no result written */
 } dpl_status;
 
+/* Element types of raster arguments that accept several. */
+typedef enum dpl_dtype {
+    DPL_DTYPE_F32 = 0,
+    DPL_DTYPE_U8 = 1,
+    DPL_DTYPE_I8 = 2,
+    DPL_DTYPE_I16 = 3,
+    DPL_DTYPE_U16 = 4,
+    DPL_DTYPE_I32 = 5
+} dpl_dtype;
+
 /* Message for the last non-OK status returned on the calling host thread. */
 const char* dpl_last_error_message(void);
 
@@ -237,6 +247,19 @@ dpl_status dpl_similarity_prep(const float* stack, int is_complex, int64_t nlaye
  * 1 <= search_radius <= dpl_similarity_max_radius(). */
 dpl_status dpl_similarity(const float* unit, int64_t nlayers, int64_t rows, int64_t cols,
                           int search_radius, int kind, float* out, dpl_stream_t stream);
+
+/* ---------------------------------------------------------------------------------
+ * Wrapped-phase workflow helpers.
+ * ------------------------------------------------------------------------------- */
+
+/* Replaces: utils.grow_nodata_region(arr, nodata, n_pixels) -- utils.py:613-660, applied
+ * to the strided outputs of each block in workflows/single.py:352-362.
+ * in, out : (rows, cols) of `dtype` (dpl_dtype); out must not alias in
+ * A pixel of out is `nodata` where any pixel of the (2 n_pixels + 1)^2 square around it
+ * (clipped to the image) is nodata in `in`, else the pixel of `in`.  Nodata means equal
+ * to `nodata`, or NaN if nodata_is_nan (integer arrays then have none). */
+dpl_status dpl_grow_nodata_region(const void* in, void* out, int dtype, int64_t rows, int64_t cols,
+                                  double nodata, int nodata_is_nan, int n_pixels, dpl_stream_t stream);
 
 /* ---------------------------------------------------------------------------------
  * Learned EMI warm start (no counterpart in the reference, whose EMI inverse iteration

@@ -339,11 +339,157 @@ def make_similarity():
     _save("similarity", **out)
 
 
+NONE_IDX = -(2**31)  # a None slice bound
+
+
+def _enc(b):
+    return [NONE_IDX if v is None else int(v) for v in (b.row_start, b.row_stop, b.col_start, b.col_stop)]
+
+
+def _ref_single(stack, hw, strides, block_shape, first_real, out_ref, comp_ref, nodata, ps, amp_mean, amp_disp,
+                shp_nslc, alpha):
+    """workflows/single.py:188-368 on arrays, with the reference's own functions; no files."""
+    rows, cols = stack.shape[1:]
+    mgr = R.blocks.StridedBlockManager(arr_shape=(rows, cols), block_shape=block_shape, strides=ST(*strides),
+                                       half_window=HW(*hw))
+    orow, ocol = rows // strides[0], cols // strides[1]
+    n = len(stack)
+    nreal = n - first_real
+    out = {
+        "pl": np.zeros((nreal, orow, ocol), np.complex64), "crlb": np.zeros((nreal, orow, ocol), np.float32),
+        "clos": np.zeros((orow, ocol, n - 2), np.float32), "comp": np.zeros((rows, cols), np.complex64),
+        "disp": np.zeros((rows, cols), np.float32), "tc": np.zeros((orow, ocol), np.float32),
+        "counts": np.zeros((orow, ocol), np.int32), "eig": np.zeros((orow, ocol), np.float32),
+        "est": np.zeros((orow, ocol), np.uint8),
+    }
+    var = (amp_disp * amp_mean) ** 2
+    for (o_r, o_c), (t_r, t_c), (i_r, i_c), (p_r, p_c), (f_r, f_c) in mgr.iter_blocks():
+        if nodata[i_r, i_c].all():
+            continue
+        cur = stack[:, i_r, i_c]
+        if np.all(cur == 0) or np.isnan(cur).all():
+            continue
+        cur = cur.astype(np.complex64)
+        nb = R.shp.estimate_neighbors(halfwin_rowcol=hw, alpha=alpha, strides=ST(*strides), mean=amp_mean[i_r, i_c],
+                                      var=var[i_r, i_c], nslc=shp_nslc, method=R.ShpMethod.GLRT)
+        try:
+            res = R.core.run_phase_linking(cur.copy(), HW(*hw), ST(*strides), reference_idx=out_ref,
+                                           nodata_mask=nodata[i_r, i_c], ps_mask=ps[i_r, i_c], neighbor_arrays=nb,
+                                           avg_mag=amp_mean[i_r, i_c], first_real_slc_idx=first_real,
+                                           compute_crlb=True)
+        except R.core.PhaseLinkRuntimeError:
+            continue
+        cpx = np.nan_to_num(np.asarray(res.cpx_phase))
+        crlb = np.nan_to_num(np.asarray(res.crlb_std_dev))
+        tcoh = np.nan_to_num(np.asarray(res.temp_coh))
+        m_, d_, _ = R.ps.calc_ps_block(np.abs(cur[first_real:, f_r, f_c]))
+        comp = np.asarray(R.compress.compress(cur[:, f_r, f_c], cpx[:, t_r, t_c], first_real_slc_idx=first_real,
+                                              slc_mean=m_, reference_idx=comp_ref))
+        part = cpx[first_real:, t_r, t_c]
+        h, w = part.shape[-2:]
+        sl = (slice(o_r.start, o_r.start + h), slice(o_c.start, o_c.start + w))
+        out["pl"][(slice(None),) + sl] = part
+        out["crlb"][(slice(None),) + sl] = crlb[first_real:, t_r, t_c]
+        out["clos"][sl] = np.asarray(res.closure_phases)[t_r, t_c]
+        ch, cw = comp.shape
+        out["comp"][p_r.start:p_r.start + ch, p_c.start:p_c.start + cw] = comp
+        out["disp"][p_r.start:p_r.start + ch, p_c.start:p_c.start + cw] = d_
+        for key, src, nd in (("tc", tcoh, 0), ("counts", np.asarray(res.shp_counts), 0),
+                             ("eig", np.asarray(res.eigenvalues), 0), ("est", np.asarray(res.estimator), 255)):
+            out[key][sl] = R.utils.grow_nodata_region(src[t_r, t_c], nodata=nd, n_pixels=2, copy=True)
+    out["sim"] = np.asarray(R.similarity.median_similarity(out["pl"].copy(), search_radius=7))
+    return out
+
+
+def make_workflow():
+    """Block manager, ministack planner and grow_nodata_region known answers, and a
+    two-ministack sequential run built from the reference's own per-block functions."""
+    import json
+    from datetime import datetime, timedelta
+
+    out = {}
+    cfgs = [((40, 50), (16, 16), (2, 2), (3, 5)), ((37, 41), (10, 12), (1, 1), (2, 3)), ((64, 64), (32, 32), (1, 1),
+                                                                                       (0, 0)),
+            ((50, 30), (20, 20), (3, 2), (4, 4)), ((25, 25), (512, 512), (1, 1), (5, 11))]
+    for k, (shape, block, strides, hw) in enumerate(cfgs):
+        mgr = R.blocks.StridedBlockManager(arr_shape=shape, block_shape=block, strides=ST(*strides),
+                                           half_window=HW(*hw))
+        rows = [sum((_enc(b) for b in blk), []) for blk in mgr.iter_blocks()]
+        out[f"blocks_{k}"] = np.array(rows, dtype=np.int64).reshape(-1, 20)
+        out[f"blocks_cfg_{k}"] = np.array(list(shape) + list(block) + list(strides) + list(hw))
+    out["nblock_cfgs"] = np.array(len(cfgs))
+
+    plans = []
+    for (n, size, max_comp, plan, out_ref) in [(11, 4, 2, "always_first", None), (10, 5, 100, "always_first", None),
+                                               (9, 3, 1, "always_first", 0), (6, 6, 5, "last_per_ministack", None),
+                                               (7, 10, 5, "always_first", 2), (15, 4, 0, "always_first", None)]:
+        files = [f"slc_{(datetime(2020, 1, 1) + timedelta(days=12 * i)).strftime('%Y%m%d')}.tif" for i in range(n)]
+        dates = [[datetime(2020, 1, 1) + timedelta(days=12 * i)] for i in range(n)]
+        planner = R.stack.MiniStackPlanner(file_list=files, dates=dates, is_compressed=[False] * n,
+                                           output_folder="ms", max_num_compressed=max_comp,
+                                           output_reference_idx=out_ref, compressed_slc_plan=plan)
+        made, comp_paths = [], []
+        for ms in planner.plan(size):
+            layers = []
+            for f in ms.file_list:
+                f = str(f)
+                layers.append(files.index(f) if f in files else -(1 + comp_paths.index(f)))
+            made.append({"layers": layers, "is_compressed": list(map(bool, ms.is_compressed)),
+                         "out_ref": int(ms.output_reference_idx), "comp_ref": int(ms.compressed_reference_idx),
+                         "first_real": int(ms.first_real_slc_idx)})
+            comp_paths.append(str(ms.get_compressed_slc_info().path))
+        plans.append({"n": n, "size": size, "max_comp": max_comp, "plan": plan, "out_ref": out_ref, "ministacks": made})
+    out["plans"] = np.array(json.dumps(plans))
+
+    rng = np.random.default_rng(901)
+    g = rng.normal(size=(14, 17)).astype(np.float32)
+    g[g < -1.2] = 0
+    g[3, 5] = 0
+    e = (rng.random((9, 11)) > 0.5).astype(np.uint8)
+    e[4, 4] = 255
+    gn = g.copy()
+    gn[7, 7] = np.nan
+    for k, (arr, nd, npx) in enumerate([(g, 0, 2), (g, 0, 1), (e, 255, 2), (gn, np.nan, 1), (e, 0, 0)]):
+        out[f"grow_in_{k}"] = arr
+        out[f"grow_nd_{k}"] = np.array(nd, dtype=np.float64)
+        out[f"grow_n_{k}"] = np.array(npx)
+        out[f"grow_out_{k}"] = R.utils.grow_nodata_region(arr, nodata=nd, n_pixels=npx, copy=True)
+    out["ngrow"] = np.array(5)
+
+    # two ministacks of 4 SLCs (the second led by the first one's compressed SLC)
+    cfg = StackConfig(nslc=8, rows=20, cols=26, seed=902, ps_frac=0.04)
+    z = make_stack(cfg)
+    amp_mean, amp_disp, ps = R.ps.calc_ps_block(np.abs(z), 0.25, cfg.nslc)
+    amp_mean, amp_disp, ps = (np.asarray(a) for a in (amp_mean, amp_disp, ps))
+    nodata = np.zeros(z.shape[1:], bool)
+    nodata[:3, :4] = True
+    hw, strides, block = (2, 3), (1, 1), (12, 12)
+    comp_list = []
+    files = [f"slc_{(datetime(2020, 1, 1) + timedelta(days=12 * i)).strftime('%Y%m%d')}.tif" for i in range(8)]
+    dates = [[datetime(2020, 1, 1) + timedelta(days=12 * i)] for i in range(8)]
+    planner = R.stack.MiniStackPlanner(file_list=files, dates=dates, is_compressed=[False] * 8, output_folder="ms",
+                                       max_num_compressed=100)
+    for k, ms in enumerate(planner.plan(4)):
+        real = [files.index(str(f)) for f in ms.file_list if str(f) in files]
+        layers = ([c for c in comp_list] if comp_list else []) + [z[i] for i in real]
+        cur = np.stack(layers).astype(np.complex64)
+        res = _ref_single(cur, hw, strides, block, int(ms.first_real_slc_idx), int(ms.output_reference_idx),
+                          int(ms.compressed_reference_idx), nodata, ps, amp_mean, amp_disp, 8, 0.05)
+        comp_list.append(res["comp"])
+        for key, val in res.items():
+            out[f"seq{k}_{key}"] = val
+        print(f"  sequential ministack {k}: {len(cur)} layers")
+    out["seq_slc"], out["seq_nodata"], out["seq_ps"] = z, nodata, ps
+    out["seq_amp_mean"], out["seq_amp_disp"] = amp_mean, amp_disp
+    out["seq_cfg"] = np.array(list(hw) + list(strides) + list(block) + [4])
+    _save("workflow", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["ps", "glrt", "ks", "covariance", "phase_link", "config1", "ps_fill", "compress",
-                             "similarity"]
+                             "similarity", "workflow"]
     for w in which:
         print(f"[{w}]")
         {"ps": make_ps, "glrt": make_glrt, "ks": make_ks, "covariance": make_covariance,
          "phase_link": make_phase_link, "config1": make_config1_crop, "ps_fill": make_ps_fill,
-         "compress": make_compress, "similarity": make_similarity}[w]()
+         "compress": make_compress, "similarity": make_similarity, "workflow": make_workflow}[w]()

@@ -413,6 +413,12 @@ def load_reference():
 
     ps = _load_file("dolphin.ps", REF_SRC / "ps.py")
     similarity = _load_file("dolphin.similarity", REF_SRC / "similarity.py")
+    # the block manager and the ministack planner (file names and dates only; the
+    # date parser of opera_utils is never reached for real SLCs given as dates)
+    blocks = _load_file("dolphin.io._blocks", REF_SRC / "io" / "_blocks.py")
+    dolphin.io.DEFAULT_DATETIME_FORMAT = "%Y%m%d"
+    _module("opera_utils", get_dates=lambda *a, **k: (_ for _ in ()).throw(NotImplementedError("get_dates")))
+    stack = _load_file("dolphin.stack", REF_SRC / "stack.py")
     incidence = load_function(REF_SRC / "timeseries.py", "get_incidence_matrix", flatten=utils.flatten)
 
     _LOADED = types.SimpleNamespace(
@@ -432,6 +438,8 @@ def load_reference():
         ps=ps,
         similarity=similarity,
         get_incidence_matrix=incidence,
+        blocks=blocks,
+        stack=stack,
         ShpMethod=enums.ShpMethod,
     )
     return _LOADED

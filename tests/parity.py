@@ -53,3 +53,43 @@ def compare_pl(out, g, prefix, tc_min=0.3, phase_tol=1e-3, tc_tol=1e-4, borderli
     np.testing.assert_allclose(out.crlb_std_dev[fin], ref["crlb_std_dev"][fin], rtol=2e-3, atol=1e-5)
     cl_err = _phase_err(np.exp(1j * out.closure_phases), np.exp(1j * ref["closure_phases"]))
     assert cl_err.max() < 1e-4
+
+
+def compare_workflow(out, ref, tc_min=0.3, phase_tol=1e-3, tc_tol=1e-4, sim_tol=2e-3, est_mismatch=0.01,
+                     eig_rtol=1e-3, crlb_rtol=2e-3):
+    """Compare one ministack's block-loop rasters (dicts with keys pl, crlb, clos, comp,
+    disp, tc, counts, eig, est, sim) with a reference run.
+
+    SHP counts and the nodata (zero) patterns must match exactly; the estimator may
+    differ on a small share of pixels whose |Gamma| is within rounding of singular.
+    Phases (linked, closure, compressed) within ``phase_tol`` rad and the temporal
+    coherence within ``tc_tol`` on pixels with coherence > ``tc_min``.
+    """
+    np.testing.assert_array_equal(np.asarray(out["counts"]).astype(np.int64), np.asarray(ref["counts"]).astype(np.int64))
+    np.testing.assert_array_equal(out["tc"] == 0, ref["tc"] == 0)
+    np.testing.assert_array_equal(out["pl"] == 0, ref["pl"] == 0)
+    good = (ref["tc"] > tc_min) & (out["tc"] > tc_min)
+    assert good.sum() > 0
+    assert np.max(np.abs(out["tc"][good] - ref["tc"][good])) <= tc_tol
+    assert np.max(phase_err(out["pl"][:, good], ref["pl"][:, good])) <= phase_tol
+    if ref["clos"].size:
+        d = np.angle(np.exp(1j * (out["clos"][good] - ref["clos"][good])))
+        assert np.max(np.abs(d)) <= phase_tol
+    mism = np.mean(np.asarray(out["est"]) != np.asarray(ref["est"]))
+    assert mism <= est_mismatch, mism
+    # eigenvalues and CRLB only where C has full rank (at least as many SHP samples as
+    # layers), as for a single phase-linking call
+    n_layers = ref["clos"].shape[-1] + 2
+    posed = good & (np.asarray(out["est"]) == np.asarray(ref["est"])) & (np.asarray(ref["counts"]) >= n_layers)
+    np.testing.assert_allclose(out["eig"][posed], ref["eig"][posed], rtol=eig_rtol, atol=1e-4)
+    np.testing.assert_allclose(out["crlb"][:, posed], ref["crlb"][:, posed], rtol=crlb_rtol, atol=1e-5)
+    # compressed SLC: mean amplitude and the phase of the projection on the linked phases
+    np.testing.assert_array_equal(np.isnan(out["comp"]), np.isnan(ref["comp"]))
+    np.testing.assert_allclose(out["disp"], ref["disp"], rtol=1e-5, atol=1e-6)
+    ok = np.isfinite(ref["comp"]) & (np.abs(ref["comp"]) > 0)
+    np.testing.assert_allclose(np.abs(out["comp"][ok]), np.abs(ref["comp"][ok]), rtol=1e-5)
+    assert np.max(phase_err(out["comp"][ok], ref["comp"][ok])) <= 5 * phase_tol
+    np.testing.assert_array_equal(np.isnan(out["sim"]), np.isnan(ref["sim"]))
+    fin = ~np.isnan(ref["sim"])
+    if fin.any():
+        assert np.max(np.abs(out["sim"][fin] - ref["sim"][fin])) <= sim_tol
