@@ -509,6 +509,78 @@ SIM_LAYERS, SIM_RADIUS, SIM_SEED = 30, 7, 20261209
 SEQ_MINISTACK = 15
 
 
+def run_learned(args):
+    """Learned EMI warm start: train the 190-256-256-40 network on 2 M pixels of N=20
+    stacks (the library's GEMM, ReLU, MSE and Adam kernels), then solve the held-out
+    4096x4096 N=20 frame (half-window (5, 11), 1024x1024 blocks) with and without the
+    warm start; the timed region per block is the solve (and, warm, the network)."""
+    import torch
+
+    from dolphin_gb300 import estimate_stack_covariance
+    from dolphin_gb300._build import build_library
+    from dolphin_gb300.learned import WarmStartMLP, make_training_set, process_coherence_warm
+    from dolphin_gb300.simulate import StackConfig, make_stack_torch
+
+    build_library()
+    n, frame = 20, args.frame
+    train_px = 2_000_000 if frame >= 2048 else 200_000
+    t0 = time.perf_counter()
+    X, T = make_training_set(train_px, nslc=n, tile=64, seed=20261300)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    model = WarmStartMLP(nslc=n, seed=0)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(0)
+    steps, batch = 3000, 4096
+    t0 = time.perf_counter()
+    losses = []
+    for _ in range(steps):
+        idx = torch.randint(0, X.shape[0], (batch,), generator=gen, device="cuda")
+        losses.append(model.train_step(X[idx].contiguous(), T[idx].contiguous(), lr=1e-3))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del X, T
+    z = make_stack_torch(StackConfig(nslc=n, rows=frame, cols=frame, seed=20261208, ps_frac=0.0))
+    plan = block_plan(frame, frame, BLOCK, HALF)
+    stream = torch.cuda.current_stream()
+    ms = {"plain": 0.0, "warm": 0.0}
+    iters = {"plain": [], "warm": []}
+    worst, px = 0.0, 0
+    for (ir, ic, *_r) in plan:
+        blk = z[:, ir[0]:ir[1], ic[0]:ic[1]].contiguous()
+        C = estimate_stack_covariance(blk, HALF).reshape(-1, n, n).contiguous()
+        res = {}
+        for kind in ("plain", "warm"):  # warm-up passes
+            res[kind] = process_coherence_warm(C, model if kind == "warm" else None)
+        for kind in ("plain", "warm"):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            torch.cuda.synchronize()
+            e[0].record(stream)
+            res[kind] = process_coherence_warm(C, model if kind == "warm" else None)
+            e[1].record(stream)
+            torch.cuda.synchronize()
+            ms[kind] += e[0].elapsed_time(e[1])
+            iters[kind].append(res[kind][5].float().mean().item())
+        v0, v1, tc = res["plain"][0], res["warm"][0], res["plain"][4]
+        good = (res["plain"][2] == 1) & (tc > 0.3)
+        d = torch.angle(v1[good] * v0[good].conj()).abs()
+        worst = max(worst, float(d.max().item()) if d.numel() else 0.0)
+        px += C.shape[0]
+        del C
+    line = {
+        "workload": "learned", "metric": "EMI solve pixels/sec (N=20) with the learned warm start vs plain",
+        "value": px / (ms["warm"] / 1000.0), "unit": UNIT, "plain": px / (ms["plain"] / 1000.0),
+        "iterations_per_pixel": {k: float(np.mean(v)) for k, v in iters.items()},
+        "max_phase_diff_rad_coh_gt_0.3": worst, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"N=20 {frame}x{frame} held-out frame (seed 20261208), half-window {HALF}, "
+                               f"{BLOCK}x{BLOCK} blocks; network 190-256-256-40 trained on {train_px} pixels",
+                   "training": {"pixels": train_px, "adam_steps": steps, "batch": batch,
+                                "loss_first_last": [float(np.mean(losses[:20])), float(np.mean(losses[-20:]))],
+                                "data_s": round(t_data, 2), "train_s": round(t_train, 2)}},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_sequential(args):
     """The sequential estimator on the 30-SLC workload: ministacks of 15 real SLCs (the
     second led by the first one's compressed SLC), 1024x1024 blocks with the (5, 11)
@@ -695,12 +767,13 @@ def main():
     ap.add_argument("--frame", type=int, default=FRAME)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--workload", default="config2",
-                    choices=["config2", "precision", "batch", "similarity", "sequential"],
+                    choices=["config2", "precision", "batch", "similarity", "sequential", "learned"],
                     help="precision: N=40 2048x2048 stack, half-window (7, 7), low gamma_inf with a "
                          "high-coherence disk; rates of the tensor-core and SIMT covariance forms. "
                          "batch: 12 ministacks of N = 8..45, 1024x1024 each, as one CUDA graph. "
                          "similarity: median phase similarity, radius 7, of 30 interferograms. "
-                         "sequential: the 30-SLC frame as ministacks of 15 with compressed SLCs")
+                         "sequential: the 30-SLC frame as ministacks of 15 with compressed SLCs. "
+                         "learned: EMI with and without the learned warm start, N=20")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -718,6 +791,9 @@ def main():
         return
     if args.workload == "sequential":
         run_sequential(args)
+        return
+    if args.workload == "learned":
+        run_learned(args)
         return
     pool = None
     cores = len(os.sched_getaffinity(0))
