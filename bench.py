@@ -444,9 +444,36 @@ def run_precision(args):
         e1.record()
         torch.cuda.synchronize()
         rates[form] = frame * frame * max(1, args.steps) / (e0.elapsed_time(e1) / 1000.0)
+    # the FP64 form (covariance and solver in double) on a 512x512 crop that holds the
+    # disk's edge: its rate, and each float32 form's error against it
+    r0 = frame // 2 - 256 + int(0.125 * frame) // 2
+    crop = stack[:, r0:r0 + 512 + 2 * half[0], r0:r0 + 512 + 2 * half[1]].contiguous()
+    cm, cd, _cps = dp.calc_ps_block(crop.abs(), PS_THR, n)
+    cnb = dp.estimate_neighbors(halfwin_rowcol=half, alpha=ALPHA, mean=cm, var=(cd * cm) ** 2, nslc=n)
+    outs, crop_rates = {}, {}
+    for form in ("fp64", "tensor", "simt"):
+        dp.run_phase_linking(crop, half, neighbor_arrays=cnb, covariance_form=form)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        outs[form] = dp.run_phase_linking(crop, half, neighbor_arrays=cnb, covariance_form=form)
+        e1.record()
+        torch.cuda.synchronize()
+        crop_rates[form] = crop.shape[1] * crop.shape[2] / (e0.elapsed_time(e1) / 1000.0)
+    ref = outs["fp64"]
+    good = ref.temp_coh > 0.3
+    errs = {}
+    for form in ("tensor", "simt"):
+        d = torch.angle(outs[form].cpx_phase[:, good] * ref.cpx_phase[:, good].conj()).abs()
+        t = (outs[form].temp_coh[good] - ref.temp_coh[good]).abs()
+        worst = d.max(0).values  # per pixel, over the SLCs
+        errs[form] = {"phase_max_rad": float(d.max()), "phase_p99_rad": float(torch.quantile(d.flatten()[:2**24], 0.99)),
+                      "pixels_above_1e-3_rad": int((worst > 1e-3).sum()), "temp_coh_max": float(t.max())}
     print(json.dumps({"workload": "precision", "config": {"nslc": n, "frame": frame, "half_window": half,
                                                           "gamma_inf": 0.02, "disk_gamma0": 0.95},
-                      "unit": UNIT, "rates": rates, "tensor_over_simt": rates["tensor"] / rates["simt"]}),
+                      "unit": UNIT, "rates": rates, "tensor_over_simt": rates["tensor"] / rates["simt"],
+                      "fp64_crop": {"pixels": int(crop.shape[1] * crop.shape[2]), "rates": crop_rates,
+                                    "coherent_pixels": int(good.sum()), "errors_vs_fp64": errs}}),
           flush=True)
 
 

@@ -163,6 +163,7 @@ struct PixArgs {
     float one_minus_beta, beta, zct;
     int ref_idx, compute_crlb, crlb_ref, baseline_lag;
     float crlb_factor;
+    double beta_d, zct_d, crlb_factor_d;  // the same parameters unrounded (FP64 form)
     cfloat* Cout;            // cov-only output: (npix, n, n)
     cfloat* vout;            // (npix, n) referenced eigenvectors
     float* eig;
@@ -320,6 +321,7 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
 
 }  // namespace dpl
 
+#include "solver64.cuh"
 #include "cov_tc.cuh"
 
 namespace dpl {
@@ -521,6 +523,27 @@ static dpl_status launch_solve_reg(const PixArgs& a, cudaStream_t s) {
 
 // Main pass (Cholesky inverse iteration) and, for the pixels it lists, the LU pass.
 // `fb` holds a counter followed by room for every pixel index.
+// FP64 form: covariance and solver in double, one warp per pixel
+static dpl_status launch_pixel64(const PixArgs& a, cudaStream_t s) {
+    const Pix64Layout L = make_layout64(a.n, a.stg);
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)(200 * 1024) / L.bytes));
+    const size_t smem = (size_t)warps * L.bytes;
+    if (smem > (size_t)227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "fp64 form: window or nslc too large");
+    int dev = 0, sms = 0;
+    DPL_CUDA_TRY(cudaGetDevice(&dev));
+    DPL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t want = (a.npix + warps - 1) / warps;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * 8));
+    if (a.n <= 32) {
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_pixel64<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_pixel64<1><<<grid, 32 * warps, smem, s>>>(a, L);
+    } else {
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_pixel64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_pixel64<2><<<grid, 32 * warps, smem, s>>>(a, L);
+    }
+    return check_launch("k_pixel64");
+}
+
 template <int MODE>
 static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr) {
     if (a.npix == 0) return DPL_OK;
@@ -623,6 +646,9 @@ static void set_solver_params(PixArgs& a, int use_evd, double beta, double zct, 
     a.compute_crlb = compute_crlb;
     a.crlb_ref = std::max(first_real - 1, 0);
     a.crlb_factor = (float)(2.0 * num_looks);
+    a.beta_d = beta;
+    a.zct_d = zct;
+    a.crlb_factor_d = 2.0 * num_looks;
 }
 
 struct PlWorkspace {
@@ -688,7 +714,7 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
     const int n = (int)P.nslc;
     const int ref = norm_ref(P.reference_idx, n);
     if (ref < 0 || ref >= n) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
-    if (P.cov_form != 0 && P.cov_form != 1) return fail(DPL_ERR_INVALID_ARGUMENT, "cov_form must be 0 or 1");
+    if (P.cov_form < 0 || P.cov_form > 2) return fail(DPL_ERR_INVALID_ARGUMENT, "cov_form must be 0, 1 or 2");
     if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
     PlWorkspace w;
@@ -733,7 +759,10 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
         a.counts = in->neighbors ? out->shp_counts : nullptr;
         TcArgs tcfit{};
         const bool tc_fits = P.cov_form == 0 && tc_configure(tcfit, n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx);
-        if (tc_fits) {
+        if (P.cov_form == 2) {
+            // FP64 form: covariance and solver in double precision
+            st = timed(s, 0, [&] { return launch_pixel64(a, s); });
+        } else if (tc_fits) {
             // chosen form: tensor-core covariance, then the solver on the planar matrices
             st = timed(s, 0, [&] {
                 return launch_cov_tc(n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, w.zt, nullptr, 0,
@@ -839,6 +868,8 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
                                      void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
     dpl_status st = validate_common(nslc, rows, cols, hy, hx, sy, sx);
     if (st != DPL_OK) return st;
+    if (cov_form != 0 && cov_form != 1)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: cov_form must be 0 or 1 (2, fp64, is a phase-linking form)");
     if (!slc || !C || !workspace) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: null pointer");
     if (workspace_bytes < dpl_covariance_workspace_size(nslc, rows, cols))
         return fail(DPL_ERR_WORKSPACE, "dpl_covariance: workspace too small");

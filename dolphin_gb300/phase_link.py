@@ -94,7 +94,9 @@ def run_phase_linking(
 
     ``covariance_form`` (keyword-only, not in the reference): ``"tensor"`` computes
     the coherence matrices on the tensor cores (bf16 hi/lo split, fp32
-    accumulation); ``"simt"`` uses fp32 CUDA-core arithmetic throughout.
+    accumulation); ``"simt"`` uses fp32 CUDA-core arithmetic throughout; ``"fp64"``
+    computes the covariance and the solve in double precision (a checker: GB300's
+    FP64 rate is low), writing the same float32 outputs.
     """
     on_device = D.is_device_tensor(slc_stack)
     shape = tuple(slc_stack.shape)
@@ -168,7 +170,7 @@ def run_phase_linking(
 
 
 def _form_code(form: str) -> int:
-    codes = {"tensor": 0, "simt": 1}
+    codes = {"tensor": 0, "simt": 1, "fp64": 2}
     if form not in codes:
         raise ValueError(f"covariance_form must be one of {sorted(codes)}, got {form!r}")
     return codes[form]

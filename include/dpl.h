@@ -118,7 +118,8 @@ typedef struct dpl_pl_params {
     int baseline_lag;              /* <= 0: off */
     int first_real_slc_idx;
     int compute_crlb;
-    int cov_form;                  /* 0: tensor-core covariance (default); 1: SIMT covariance (plain form) */
+    int cov_form;                  /* 0: tensor-core covariance (default); 1: SIMT covariance (plain form);
+                                      2: covariance and solver in FP64 (the double-precision checker) */
 } dpl_pl_params;
 
 typedef struct dpl_pl_inputs {

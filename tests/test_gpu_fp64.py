@@ -1,0 +1,94 @@
+"""FP64 form (covariance and solver in double on the GPU) against the float64 oracle.
+
+Both compute in double; the GPU writes float32 outputs, so phases agree to float32
+rounding (~1e-7 rad) and the temporal coherence to ~1e-7.  Pixels whose |Gamma| +
+1e-6 I has a smallest eigenvalue below 1e-9 (where even double rounding decides the
+Cholesky outcome) are left out of the estimator comparison; eigenvalues and CRLB are
+compared where C has full rank.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import phase_link as O
+from parity import phase_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover - CPU container
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import dolphin_gb300 as dp  # noqa: E402
+from dolphin_gb300.simulate import StackConfig, make_stack  # noqa: E402
+
+
+def _compare(out, ref, diag, counts_ok, phase_tol=2e-6, tc_tol=2e-6):
+    keep = diag["gamma_min_eig"] >= 1e-9
+    np.testing.assert_array_equal(out.estimator[keep], ref.estimator[keep])
+    np.testing.assert_array_equal(np.isnan(out.temp_coh), np.isnan(ref.temp_coh))
+    fin = keep & np.isfinite(ref.temp_coh) & np.all(np.isfinite(ref.cpx_phase), axis=0)
+    assert fin.sum() > 0
+    err = phase_err(out.cpx_phase[:, fin], ref.cpx_phase[:, fin].astype(np.complex64))
+    assert err.max() <= phase_tol, err.max()
+    assert np.abs(out.temp_coh[fin] - ref.temp_coh[fin]).max() <= tc_tol
+    posed = fin & counts_ok
+    np.testing.assert_allclose(out.eigenvalues[posed], ref.eigenvalues[posed], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(out.crlb_std_dev[:, posed], ref.crlb_std_dev[:, posed], rtol=1e-4, atol=1e-6)
+    if ref.closure_phases.size:
+        cl = phase_err(np.exp(1j * out.closure_phases[fin]), np.exp(1j * ref.closure_phases[fin]))
+        assert cl.max() <= 1e-5
+
+
+def test_fp64_precision_case():
+    hw = (7, 7)
+    cfg = StackConfig(nslc=40, rows=40 + 14, cols=44 + 14, seed=20261206, gamma_inf=0.02, disk_gamma0=0.95,
+                      disk_radius=0.3, ps_frac=0.0)
+    z = make_stack(cfg)
+    mean, disp, _ps = dp.calc_ps_block(np.abs(z), 0.25, cfg.nslc)
+    nb = dp.estimate_neighbors(halfwin_rowcol=hw, alpha=0.001, mean=mean, var=(disp * mean) ** 2, nslc=cfg.nslc)
+    diag = {}
+    ref = O.run_phase_linking(z, hw, neighbor_arrays=nb, dtype=np.float64, diagnostics=diag)
+    out = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form="fp64")
+    np.testing.assert_array_equal(out.shp_counts, ref.shp_counts)
+    _compare(out, ref, diag, ref.shp_counts >= cfg.nslc)
+    # the float32 forms against it: the precision table's denominator on the GPU
+    for form in ("tensor", "simt"):
+        o32 = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form=form)
+        good = (out.temp_coh > 0.3) & (diag["gamma_min_eig"] >= 1e-3)
+        err = phase_err(o32.cpx_phase[:, good], out.cpx_phase[:, good])
+        print(f"[fp64] form={form:6s} vs GPU float64: phase err max {err.max():.2e} rad on {good.sum()} pixels")
+        assert err.max() < 1e-3
+
+
+@pytest.mark.parametrize("kw", [
+    dict(),
+    dict(strides=(2, 3)),
+    dict(use_evd=True),
+    dict(beta=0.1, zero_correlation_threshold=0.05),
+    dict(baseline_lag=4),
+    dict(reference_idx=3, first_real_slc_idx=2),
+])
+def test_fp64_options_against_oracle(kw):
+    cfg = StackConfig(nslc=10, rows=30, cols=34, seed=20261204, ps_frac=0.05)
+    z = make_stack(cfg)
+    z[2, 4, 5] = np.nan
+    z[:, 10, 11] = np.nan
+    mean, disp, ps = dp.calc_ps_block(np.abs(z), 0.25, cfg.nslc)
+    hw = (5, 5)
+    strides = kw.pop("strides", (1, 1))
+    nb = dp.estimate_neighbors(halfwin_rowcol=hw, alpha=0.001, strides=strides, mean=mean, var=(disp * mean) ** 2,
+                               nslc=cfg.nslc)
+    diag = {}
+    ref = O.run_phase_linking(z, hw, strides, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, dtype=np.float64,
+                              diagnostics=diag, **kw)
+    out = dp.run_phase_linking(z, hw, strides, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean,
+                               covariance_form="fp64", **kw)
+    np.testing.assert_array_equal(out.shp_counts, ref.shp_counts)
+    _compare(out, ref, diag, ref.shp_counts >= cfg.nslc)
+
+
+def test_fp64_rejected_by_covariance_entry():
+    z = make_stack(StackConfig(nslc=4, rows=8, cols=8, seed=1, ps_frac=0.0))
+    with pytest.raises(ValueError):
+        dp.estimate_stack_covariance(z, (1, 1), covariance_form="fp64")
