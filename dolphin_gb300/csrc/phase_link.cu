@@ -562,10 +562,6 @@ static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr) {
 }
 
 // Tensor-core covariance: fills `Cg` (npix x n*n planar floats).
-static size_t tc_cov_bytes(int n, int64_t out_rows, int64_t out_cols) {
-    return (size_t)out_rows * out_cols * n * n * sizeof(float);
-}
-
 // Tile, pass and shared-memory plan of the tensor-core covariance.  False if the
 // shape does not fit (then the plain SIMT form is used).
 static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, int sy, int sx) {

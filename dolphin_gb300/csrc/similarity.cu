@@ -320,7 +320,8 @@ __device__ __forceinline__ uint32_t sim_kth(const uint32_t (&key)[D], int zeros,
             t = L + ((U - L) >> 1) + 1u;
         } else {
             const float lv = sim_unkey(L), uv = sim_unkey(U);
-            const float f = ((float)(k - below) + 0.5f) / (float)max(upto - below, 1);
+            // any pivot in [L + 1, U] is correct; the fraction only steers it
+            const float f = __fdividef((float)(k - below) + 0.5f, (float)max(upto - below, 1));
             t = min(max(sim_key(fmaf(uv - lv, f, lv)), L + 1u), U);
         }
         const int c_lane = sim_count_below<D>(key, t) - zeros;
