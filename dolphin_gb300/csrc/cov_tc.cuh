@@ -327,11 +327,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             const int e0 = pass * 2 * kTcM;
             const int e1 = min(e0 + 2 * kTcM, nn);
             const int mt = e1 - e0 > kTcM ? 2 : 1;  // M tiles holding components
-            // units: diagonal components [dlo, dhi), pairs [plo, phi) meeting [e0, e1)
-            const int dlo = min(e0, n), dhi = min(e1, n);
-            const int plo = (max(e0, n) - n) >> 1;
-            const int phi = e1 > n ? (e1 - n + 1) >> 1 : plo;
-            const int nd = dhi - dlo;
             if (builder) {
                 const int btid = tid;
                 if (!bulk) tc_prefetch(a, zbuf(0), soff, 0, btid);
