@@ -131,30 +131,44 @@ __global__ void __launch_bounds__(256) k_glrt(const __grid_constant__ CUtensorMa
     const float nslc = (float)a.nslc;
     const int W = wy * wx;
     if (!kBits) {
-        // one output byte per iteration; a tile row of pixels is one contiguous segment
+        // per output row of the tile: one item per (pixel, window row) computes the
+        // row's wx bytes into shared memory (index arithmetic once per item, the valid
+        // column range hoisted), then the row's contiguous segment of the output is
+        // written with consecutive bytes per consecutive threads (coalesced)
+        uint8_t* ob = reinterpret_cast<uint8_t*>(lg + n_tile);
+        const int tc = oc1 - oc0;
         for (int orow = or0; orow < or1; ++orow) {
             const int in_r = a.sy / 2 + orow * a.sy;
             const int r0 = clamp_start(in_r, a.hy, wy, a.rows);
             const int ur0 = in_r - a.hy;
-            const int64_t seg0 = ((int64_t)orow * a.out_cols + oc0) * W;
-            const int seg_len = (oc1 - oc0) * W;
-            for (int k = threadIdx.x; k < seg_len; k += blockDim.x) {
-                const int pix = k / W, off = k - pix * W;
-                const int wa = off / wx, wb = off - wa * wx;
+            for (int it = threadIdx.x; it < tc * wy; it += blockDim.x) {
+                const int pix = it / wy, wa = it - pix * wy;
                 const int in_c = a.sx / 2 + (oc0 + pix) * a.sx;
                 const int c0 = clamp_start(in_c, a.hx, wx, a.cols);
                 const int uc0 = in_c - a.hx;
-                const bool valid = (wa >= -ur0) && (wa < a.rows - ur0) && (wb >= -uc0) && (wb < a.cols - uc0);
-                bool shp = false;
-                if (valid && !(wa == a.hy && wb == a.hx)) {
-                    const int i1 = (in_r - rr0) * a.box_w + (in_c - x0);
-                    const int i2 = (r0 + wa - rr0) * a.box_w + (c0 + wb - x0);
-                    const float pooled = fdiv(fadd(raw[i1], raw[i2]), 2.f);
-                    const float stat = fmul(nslc, fsub(fsub(fmul(2.f, logf(pooled)), lg[i1]), lg[i2]));
-                    shp = a.thr > stat;
+                uint8_t* dst = ob + pix * W + wa * wx;
+                const bool row_ok = (wa >= -ur0) && (wa < a.rows - ur0);
+                // valid window columns of the unclamped origin
+                const int wb0 = row_ok ? max(0, -uc0) : wx, wb1 = row_ok ? min(wx, a.cols - uc0) : wx;
+                const int i1 = (in_r - rr0) * a.box_w + (in_c - x0);
+                const float s1 = raw[i1], l1 = lg[i1];
+                const float* rraw = raw + (r0 + wa - rr0) * a.box_w + (c0 - x0);
+                const float* rlg = lg + (r0 + wa - rr0) * a.box_w + (c0 - x0);
+                for (int wb = 0; wb < wx; ++wb) {
+                    bool shp = false;
+                    if (wb >= wb0 && wb < wb1 && !(wa == a.hy && wb == a.hx)) {
+                        // (s1 + s2) / 2 == (s1 + s2) * 0.5 exactly in IEEE arithmetic
+                        const float pooled = fmul(fadd(s1, rraw[wb]), 0.5f);
+                        const float stat = fmul(nslc, fsub(fsub(fmul(2.f, logf(pooled)), l1), rlg[wb]));
+                        shp = a.thr > stat;
+                    }
+                    dst[wb] = shp ? 1 : 0;
                 }
-                a.is_shp[seg0 + k] = shp ? 1 : 0;
             }
+            __syncthreads();
+            const int64_t seg0 = ((int64_t)orow * a.out_cols + oc0) * W;
+            for (int k = threadIdx.x; k < tc * W; k += blockDim.x) a.is_shp[seg0 + k] = ob[k];
+            __syncthreads();
         }
     } else {
         // one window row (<= 64 offsets) per iteration, packed into words_per_row words
@@ -369,7 +383,9 @@ dpl_status launch_glrt(const float* mean, const float* var, int64_t rows, int64_
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(DPL_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-    size_t smem = (size_t)2 * a.box_w * a.box_h * sizeof(float) + 128;
+    // staged scale^2 and its log, then one output row of byte masks
+    size_t smem = (size_t)2 * a.box_w * a.box_h * sizeof(float) + 128 + (bits ? 0 : (size_t)tc * wy * wx);
+    if (smem > (size_t)227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "GLRT window too large for shared memory");
     dim3 grid(ceil_div(a.out_cols, tc), ceil_div(a.out_rows, tr));
     if (bits) {
         DPL_CUDA_TRY(cudaFuncSetAttribute(k_glrt<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
