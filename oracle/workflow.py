@@ -2,7 +2,7 @@
 (ORACLE, test infrastructure).
 
 Follows workflows/single.py:188-368 (per block: SHP selection by GLRT on the given
-amplitude mean and dispersion, phase linking, NaN -> 0, the compressed SLC of the real
+amplitude mean and dispersion or by KS on the block's amplitudes, phase linking, NaN -> 0, the compressed SLC of the real
 SLCs with their mean and dispersion, trimmed results placed at the block's output
 position, the strided ones eroded by grow_nodata_region, 2 pixels; then the median
 similarity, radius 7), io/_blocks.py:59-348 (the block grid) and
@@ -81,7 +81,7 @@ def _sl(a, b):
 
 
 def single(stack, hw, strides, block_shape, first_real, out_ref, comp_ref, nodata, ps, amp_mean, amp_disp,
-           shp_nslc, alpha, radius=7):
+           shp_nslc, alpha, radius=7, method="glrt"):
     stack = np.asarray(stack)
     n, rows, cols = stack.shape
     sy, sx = strides
@@ -101,7 +101,8 @@ def single(stack, hw, strides, block_shape, first_real, out_ref, comp_ref, nodat
         if np.all(cur == 0) or np.isnan(cur).all():
             continue
         nb = P.estimate_neighbors(halfwin_rowcol=hw, alpha=alpha, strides=strides, mean=amp_mean[ir, ic],
-                                  var=var[ir, ic], nslc=shp_nslc, method="glrt")
+                                  var=var[ir, ic], nslc=shp_nslc,
+                                  amp_stack=np.abs(cur) if method == "ks" else None, method=method)
         try:
             res = P.run_phase_linking(cur, hw, strides, reference_idx=out_ref, nodata_mask=nodata[ir, ic],
                                       ps_mask=ps[ir, ic], neighbor_arrays=nb, avg_mag=amp_mean[ir, ic],
@@ -129,14 +130,15 @@ def single(stack, hw, strides, block_shape, first_real, out_ref, comp_ref, nodat
     return out
 
 
-def sequential(stack, size, hw, strides, block_shape, nodata, ps, amp_mean, amp_disp, alpha=0.05, max_comp=100):
+def sequential(stack, size, hw, strides, block_shape, nodata, ps, amp_mean, amp_disp, alpha=0.05, max_comp=100,
+               method="glrt"):
     """Per-ministack outputs, then the averages and the last ministack's radius-11 similarity."""
     stack = np.asarray(stack)
     comps, outs = [], []
     for layers, flags, oref, cref in plan(len(stack), size, max_comp):
         cur = np.stack([comps[-l - 1] if l < 0 else stack[l] for l in layers])
         res = single(cur, hw, strides, block_shape, flags.index(False), oref, cref, nodata, ps, amp_mean, amp_disp,
-                     len(stack), alpha)
+                     len(stack), alpha, method=method)
         comps.append(res["comp"])
         outs.append(res)
     extra = {}

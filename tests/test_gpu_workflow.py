@@ -136,6 +136,30 @@ def test_strided_three_ministacks_against_oracle():
     np.testing.assert_array_equal(_np(res.shp_counts[-1]), extra["counts_avg"])
 
 
+def test_ks_shps_against_oracle():
+    """The block loop with KS SHPs (on each block's own amplitudes) and strides (1, 2)."""
+    cfg = StackConfig(nslc=12, rows=34, cols=40, seed=905, ps_frac=0.03)
+    z = make_stack(cfg)
+    from oracle import phase_link as OP
+
+    mean, disp, ps = OP.calc_ps_block(np.abs(z), 0.25, cfg.nslc)
+    nodata = np.zeros(z.shape[1:], bool)
+    hw, strides, block, size = (2, 3), (1, 2), (16, 20), 6
+    outs, _extra = OW.sequential(z, size, hw, strides, block, nodata, ps, mean, disp, alpha=0.05, method="ks")
+    res = W.run_wrapped_phase_sequential(z, ministack_size=size, half_window=hw, strides=strides, block_shape=block,
+                                         nodata_mask=nodata, ps_mask=ps, amp_mean=mean, amp_dispersion=disp,
+                                         shp_method="ks", shp_alpha=0.05)
+    real = [len(p.layers) for p in res.ministacks]
+    pl = np.split(_np(res.pl_slcs), np.cumsum(real)[:-1])
+    crlb = np.split(_np(res.crlb), np.cumsum(real)[:-1])
+    for k, ref in enumerate(outs):
+        got = {"pl": pl[k], "crlb": crlb[k], "clos": _np(res.closure_phases[k]), "comp": _np(res.comp_slcs[k]),
+               "disp": _np(res.amp_dispersion[k]), "tc": _np(res.temp_coh[k]),
+               "counts": _np(res.shp_counts[k].to(torch.int32)), "eig": _np(res.eigenvalues[k]),
+               "est": _np(res.estimator[k]), "sim": _np(res.similarity[k])}
+        compare_workflow(got, ref, est_mismatch=EST_MISMATCH, eig_rtol=EIG_RTOL, crlb_rtol=CRLB_RTOL)
+
+
 def test_blocks_skipped_like_the_reference():
     """A block whose padded input is all zero or all NaN is skipped: its output stays 0,
     as in a freshly created raster.  (Zeros inside a processed block are not skipped:
