@@ -83,6 +83,9 @@ SIGNATURES = {
     "dpl_mse_grad": (_i, [_p, _p, _p, _i64, _p, _p]),
     "dpl_colsum": (_i, [_p, _i, _i, _p, _p]),
     "dpl_adam": (_i, [_p, _p, _p, _p, _i64, _f, _f, _f, _f, _i, _p]),
+    "dpl_mlp_packed_bytes": (_sz, [_i, _i]),
+    "dpl_mlp_pack": (_i, [_p, _i, _i, _p, _p]),
+    "dpl_mlp_forward_tc": (_i, [_p, _i64, _i, _i, _i, _i, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "dpl_process_coherence_noalloc_max_pixels": (_i64, []),
     "dpl_process_coherence_noalloc": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p]),
     "dpl_kernel_timing": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

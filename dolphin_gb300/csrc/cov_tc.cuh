@@ -35,6 +35,8 @@
 
 #include <cuda_bf16.h>
 
+#include "tc_common.cuh"
+
 namespace dpl {
 
 constexpr int kTcM = 128;                    // components per M tile
@@ -45,7 +47,6 @@ constexpr int kTcThreads = 512;              // 16 warps
 constexpr int kTcBuilders = 480;             // warps 0-14; warp 15 issues the MMAs
 constexpr int kTcCols = 512;                 // TMEM columns: two M tiles x 256 pixels
 constexpr int kTcStageBytes = 4 * 8192 + 16384;  // KR hi/lo of two M tiles + mask
-constexpr uint32_t kTcWaitLimit = 1u << 25;  // polls (>= 64 ns apart): a few seconds
 
 struct TcArgs {
     int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
@@ -67,47 +68,6 @@ struct TcArgs {
 
 constexpr int kTcRuns = 3;  // contiguous runs of image samples per K chunk (a chunk spans <= 3 region rows)
 constexpr int kTcZBuf = 4;  // ring of chunk sample buffers (bulk prefetch distance)
-
-__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-    d |= (uint64_t)1 << 46;  // descriptor version for tcgen05; swizzle none
-    return d;
-}
-
-__device__ __forceinline__ uint32_t tc_idesc_bf16(int m, int nn) {
-    uint32_t d = 0;
-    d |= 1u << 4;   // D: f32
-    d |= 1u << 7;   // A: bf16
-    d |= 1u << 10;  // B: bf16
-    d |= (uint32_t)(nn >> 3) << 17;
-    d |= (uint32_t)(m >> 4) << 24;
-    return d;
-}
-
-__device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ bool tc_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(tc_smem(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait with a short sleep between polls (a spinning thread would take issue
-// slots from the warps it waits for); returns false on timeout
-__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t it = 0; it < kTcWaitLimit; ++it) {
-        if (tc_try_wait(bar, parity)) return true;
-        __nanosleep(64);
-    }
-    return false;
-}
 
 // byte offset of element (row, k) in a K-major no-swizzle tile with KC columns
 __device__ __forceinline__ int tc_off(int row, int k) {
@@ -145,17 +105,6 @@ __device__ __forceinline__ uint4 tc_expand8(uint32_t b) {
     return r;
 }
 
-__device__ __forceinline__ void tc_ld32(uint32_t addr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(addr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 // Prefetch the samples of chunk `ch` into zs[k][t] (builder threads; soff = element
 // offset of each region sample in zt, or -1 outside the image: zero-filled).

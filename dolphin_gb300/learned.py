@@ -70,6 +70,7 @@ class WarmStartMLP:
             self.W.append(torch.from_numpy(w).cuda())
             self.b.append(torch.zeros(b, dtype=torch.float32, device="cuda"))
         self._adam = None
+        self._packed = None  # bf16 tensor-core copies of the weights (rebuilt after a change)
         self.step = 0
 
     # ---- plumbing -------------------------------------------------------------------
@@ -92,6 +93,39 @@ class WarmStartMLP:
             outs.append(out)
             h = out
         return outs
+
+    def tensor_core_ok(self) -> bool:
+        """The tensor-core forward needs two hidden layers and widths of at most 256."""
+        return len(self.W) == 3 and max(self.sizes) <= 256
+
+    def forward_tc(self, X):
+        """Network output Y (npix, 2N) float32 on the tensor cores (bf16 operands, fp32
+        accumulation): inference only."""
+        torch = D.require_cuda()
+        lib = _lib.load()
+        if not self.tensor_core_ok():
+            raise ValueError("the tensor-core forward needs two hidden layers of width <= 256")
+        if self._packed is None:
+            packed = []
+            for W in self.W:
+                nout, nin = W.shape
+                buf = torch.empty(int(lib.dpl_mlp_packed_bytes(nout, nin)), dtype=torch.uint8, device=W.device)
+                _check(lib.dpl_mlp_pack(D.ptr(W.contiguous()), nout, nin, D.ptr(buf), D.stream_handle()),
+                       "dpl_mlp_pack")
+                packed.append(buf)
+            self._packed = packed
+        X = X.contiguous()
+        npix = X.shape[0]
+        Y = torch.empty((npix, self.sizes[-1]), dtype=torch.float32, device=X.device)
+        status = torch.zeros(1, dtype=torch.int32, device=X.device)
+        s = self.sizes
+        _check(lib.dpl_mlp_forward_tc(D.ptr(X), npix, s[0], s[1], s[2], s[3], D.ptr(self._packed[0]), D.ptr(self.b[0]),
+                                      D.ptr(self._packed[1]), D.ptr(self.b[1]), D.ptr(self._packed[2]),
+                                      D.ptr(self.b[2]), D.ptr(Y), D.ptr(status), D.stream_handle()),
+               "dpl_mlp_forward_tc")
+        if int(status.item()) != 0:
+            _check(int(status.item()), "dpl_mlp_forward_tc")
+        return Y
 
     def gradients(self, X, T):
         """(loss parts, [(dW_l, db_l)]) of the mean squared error of forward(X) against T."""
@@ -133,6 +167,7 @@ class WarmStartMLP:
         if self._adam is None:
             self._adam = [(torch.zeros_like(p), torch.zeros_like(p)) for pair in zip(self.W, self.b) for p in pair]
         self.step += 1
+        self._packed = None
         params = [p for pair in zip(self.W, self.b) for p in pair]
         gradl = [g for pair in grads for g in pair]
         for p, g, (m1, m2) in zip(params, gradl, self._adam):
@@ -144,10 +179,12 @@ class WarmStartMLP:
         """Network input from coherence matrices: layout 1 = (npix, N, N) complex64."""
         return _features(C, self.nslc, layout)
 
-    def predict(self, C):
+    def predict(self, C, tensor_cores: bool = True):
         """Starting vectors (npix, N) complex64 for (npix, N, N) coherence matrices C: the
-        network's output, in the frame of C's phases relative to SLC 0."""
-        Y = self.forward(self.features(C, 1))[-1]
+        network's output (on the tensor cores where the shape allows), in the frame of
+        C's phases relative to SLC 0."""
+        X = self.features(C, 1)
+        Y = self.forward_tc(X) if tensor_cores and self.tensor_core_ok() else self.forward(X)[-1]
         return _frame(C, D.torch().view_as_complex(Y.view(-1, self.nslc, 2).contiguous()), 0)
 
     def state(self):
@@ -158,7 +195,7 @@ class WarmStartMLP:
         torch = D.require_cuda()
         self.W = [torch.from_numpy(np.asarray(state[f"W{k}"], np.float32)).cuda() for k in range(len(self.W))]
         self.b = [torch.from_numpy(np.asarray(state[f"b{k}"], np.float32)).cuda() for k in range(len(self.b))]
-        self._adam, self.step = None, 0
+        self._adam, self.step, self._packed = None, 0, None
 
 
 def make_training_set(npix_target, nslc=20, half_window=(5, 11), tile=64, seed=20261300):

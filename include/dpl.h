@@ -310,6 +310,19 @@ dpl_status dpl_colsum(const float* X, int M, int N, float* out, dpl_stream_t str
 dpl_status dpl_adam(float* w, const float* grad, float* m, float* v, int64_t count, float lr,
                     float b1, float b2, float eps, int step, dpl_stream_t stream);
 
+/* Tensor-core inference of a three-layer network (bf16 operands, fp32 accumulation in
+ * tensor memory): Y = L3(relu(L2(relu(L1(X))))), L(h) = h W^T + b, every width 1..256.
+ * dpl_mlp_pack converts one layer's W (nout, nin) fp32 into the packed bf16 blocks the
+ * forward pass streams (dpl_mlp_packed_bytes(nout, nin) bytes, 16-byte aligned).
+ * X (npix, n0) fp32, Y (npix, n3) fp32 out, b_l (n_l) fp32; status: one device int,
+ * set to DPL_ERR_TIMEOUT if a bounded wait gave up (the caller zeroes and reads it). */
+size_t dpl_mlp_packed_bytes(int nout, int nin);
+dpl_status dpl_mlp_pack(const float* W, int nout, int nin, void* packed, dpl_stream_t stream);
+dpl_status dpl_mlp_forward_tc(const float* X, int64_t npix, int n0, int n1, int n2, int n3,
+                              const void* W1, const float* b1, const void* W2, const float* b2,
+                              const void* W3, const float* b3, float* Y, int* status,
+                              dpl_stream_t stream);
+
 /* No counterpart in the reference: dpl_process_coherence without a caller-supplied
  * workspace, for callers that cannot allocate device memory per call (a C/GDAL-style
  * host that owns no device allocator and cannot size one, or a multi-stream pipeline

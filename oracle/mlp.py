@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["adam_step", "backward", "features", "forward", "mse"]
+__all__ = ["adam_step", "backward", "bf16", "features", "forward", "forward_bf16", "mse"]
 
 
 def features(C):
@@ -60,3 +60,24 @@ def adam_step(w, g, m, v, lr, b1, b2, eps, t):
     mh = m / (1 - b1**t)
     vh = v / (1 - b2**t)
     w[...] = w - lr * mh / (np.sqrt(vh) + eps)
+
+
+def bf16(x):
+    """Round float32 values to bfloat16 (nearest, ties to even), returned as float32."""
+    u = np.asarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def forward_bf16(X, weights, biases):
+    """The output of a network whose inputs, weights and hidden activations are rounded
+    to bfloat16, with exact (float64) accumulation and float32 biases: what a bf16
+    tensor-core forward pass computes up to its fp32 accumulation order."""
+    h = bf16(X).astype(np.float64)
+    for k, (W, b) in enumerate(zip(weights, biases)):
+        z = h @ bf16(W).astype(np.float64).T + np.asarray(b, np.float32)
+        if k < len(weights) - 1:
+            h = bf16(np.maximum(z, 0).astype(np.float32)).astype(np.float64)
+        else:
+            h = z
+    return h

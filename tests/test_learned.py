@@ -60,6 +60,34 @@ def test_adam_step_matches_oracle():
         np.testing.assert_allclose(st[f"W{k}"], w, rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("nslc,hidden,npix", [(20, (256, 256), 1000), (6, (100, 60), 300), (4, (16, 32), 129)])
+def test_tensor_core_forward_matches_bf16_oracle(nslc, hidden, npix):
+    """The tcgen05 forward pass against the network with bf16 inputs, weights and hidden
+    activations (float64 accumulation): they differ by the fp32 accumulation order and
+    the rare bf16 rounding it flips, well under 1 % of the output scale."""
+    model = WarmStartMLP(nslc=nslc, hidden=hidden, seed=11)
+    rng = np.random.default_rng(nslc)
+    st = model.state()
+    nl = len(hidden) + 1
+    model.load_state({**{f"W{k}": st[f"W{k}"] for k in range(nl)},
+                      **{f"b{k}": rng.normal(scale=0.1, size=st[f"W{k}"].shape[0]) for k in range(nl)}})
+    X = rng.random((npix, nslc * (nslc - 1) // 2)).astype(np.float32)
+    for _ in range(2):
+        st = model.state()
+        Ws = [st[f"W{k}"] for k in range(nl)]
+        bs = [st[f"b{k}"] for k in range(nl)]
+        got = model.forward_tc(torch.from_numpy(X).cuda()).cpu().numpy()
+        ref = M.forward_bf16(X, Ws, bs)
+        scale = np.abs(ref).max()
+        assert got.shape == ref.shape
+        assert np.abs(got - ref).max() <= 5e-3 * scale
+        ref32 = M.forward(X.astype(np.float64), [w.astype(np.float64) for w in Ws], [b.astype(np.float64) for b in bs])[-1]
+        assert np.abs(got - ref32).max() <= 3e-2 * scale
+        # a training step changes the weights: the packed copies must follow
+        T = rng.normal(size=(npix, 2 * nslc)).astype(np.float32)
+        model.train_step(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), lr=1e-2)
+
+
 def test_features_layouts_match_oracle():
     z = make_stack_torch(StackConfig(nslc=6, rows=12, cols=14, seed=5, ps_frac=0.0))
     C = dp.estimate_stack_covariance(z, (2, 2)).reshape(-1, 6, 6).contiguous()
