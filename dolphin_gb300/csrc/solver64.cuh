@@ -17,7 +17,7 @@
 //   in float32 like every other form.
 // It is the double-precision reference of the library (the arithmetic of a float64
 // run of the reference's algorithm) and the FP64 variant of the precision study;
-// GB300's FP64 rate makes it a checker, not a production form.
+// GB300's FP64 rate makes it a reference form, not a production one.
 #pragma once
 
 namespace dpl {

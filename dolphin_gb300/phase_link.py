@@ -95,7 +95,7 @@ def run_phase_linking(
     ``covariance_form`` (keyword-only, not in the reference): ``"tensor"`` computes
     the coherence matrices on the tensor cores (bf16 hi/lo split, fp32
     accumulation); ``"simt"`` uses fp32 CUDA-core arithmetic throughout; ``"fp64"``
-    computes the covariance and the solve in double precision (a checker: GB300's
+    computes the covariance and the solve in double precision (a reference form: GB300's
     FP64 rate is low), writing the same float32 outputs.
     """
     on_device = D.is_device_tensor(slc_stack)

@@ -119,7 +119,7 @@ typedef struct dpl_pl_params {
     int first_real_slc_idx;
     int compute_crlb;
     int cov_form;                  /* 0: tensor-core covariance (default); 1: SIMT covariance (plain form);
-                                      2: covariance and solver in FP64 (the double-precision checker) */
+                                      2: covariance and solver in FP64 (the double-precision reference form) */
 } dpl_pl_params;
 
 typedef struct dpl_pl_inputs {

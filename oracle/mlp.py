@@ -1,7 +1,7 @@
 """Numpy restatement of the warm-start network (ORACLE, test infrastructure).
 
 The network has no counterpart in the reference (whose EMI iteration starts from a
-constant vector, phase_link/_eigenvalues.py:139-205): this module is the checker for
+constant vector, phase_link/_eigenvalues.py:139-205): this module is the oracle for
 the GPU kernels that train and run it.  A fully connected network with ReLU on the
 hidden layers, weights W_l of shape (out, in), biases b_l, mean-squared-error loss
 over all outputs, and Adam (Kingma & Ba 2015) with bias correction.
