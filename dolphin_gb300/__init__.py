@@ -11,6 +11,9 @@ Public entry points keep the reference's names, arguments and outputs:
 * :func:`run_wrapped_phase_single`, :func:`run_wrapped_phase_sequential` (the block
   loop of dolphin.workflows.single / .sequential on device arrays, without raster I/O)
 
+:func:`deferred_checks` (not in the reference) lets a block loop of device-resident
+``run_phase_linking`` calls run without a host synchronisation per call.
+
 All compute runs in hand-written CUDA kernels for sm_103a behind the C ABI in
 ``include/dpl.h`` (``dolphin_gb300/_lib/libdpl.so``).  Importing this package
 does not initialise CUDA, so it is safe in spawned worker processes.
@@ -25,6 +28,7 @@ from .phase_link import (
     EstimatorType,
     PhaseLinkOutput,
     PhaseLinkRuntimeError,
+    deferred_checks,
     estimate_stack_covariance,
     process_coherence_matrices,
     run_phase_linking,
@@ -51,6 +55,7 @@ __all__ = [
     "StridedBlockManager",
     "calc_ps_block",
     "compress",
+    "deferred_checks",
     "estimate_neighbors",
     "estimate_stack_covariance",
     "get_circle_idxs",

@@ -6,29 +6,31 @@
 //
 //   KR[e][s]  the real components of the per-sample outer product z(s) z(s)^H
 //             (Khatri-Rao rows, the MMA's A operand, 128 rows per M tile):
-//             e <  N                  |z_i|^2                     (diagonal)
-//             e =  N + 2o, N + 2o + 1 Re, Im of z_i conj(z_j) for the lower pair
-//                                     o = i(i-1)/2 + j, i > j
+//             |z_i|^2 (diagonal), Re and Im of z_i conj(z_j) for each lower pair i > j
 //   M[p][s]   0/1: sample s of the tile's input region lies in pixel p's (clamped)
 //             window and is an SHP of p (the B operand, N = 256 pixels; exact in bf16)
 //
 // KR is split into bf16 hi + lo parts (x = hi + lo + O(2^-17 x)); both products
-// accumulate into one fp32 accumulator in tensor memory.  A pass covers 256
-// components (two M tiles, 2 x 256 TMEM columns); the diagonal is in the first pass,
-// so every pass is normalised on the fly (covariance.py:131-142: C = numer /
+// accumulate into one fp32 accumulator in tensor memory.  A pass fills two M tiles
+// (2 x 256 TMEM columns) row by row: in pass 0 rows 0 .. N-1 of M tile 0 hold the
+// diagonal; every other used row holds one lower pair, its real part in M tile 0 and
+// its imaginary part in the same row of M tile 1, so one builder thread forms both
+// from one pair of sample loads.  kTcRows = 120 rows per pass keep the Khatri-Rao work
+// of a K chunk at one item per builder thread.  The diagonal is in the first pass, so
+// every pass is normalised on the fly (covariance.py:131-142: C = numer /
 // sqrt(amp_i amp_j) where that is > 1e-6, evaluated as numer * r_i * r_j with
 // r = 1 / sqrt(amp), valid where r_i r_j < 1e6).
 //
 // Per tile the masks are turned once into per-pixel bit arrays over the region's
-// samples.  Per K chunk of 32 samples, warps 0-14 (builders) expand the chunk's mask
-// bits to bf16, form the KR rows of the pass from the chunk's samples (prefetched
-// into shared memory with cp.async while the previous chunk was built) and signal
-// the stage's `full` mbarrier; warp 15 waits on it, issues the MMAs (canonical
-// K-major no-swizzle layout: 8-row x 16-byte core matrices, LBO 128 B, SBO 512 B) and
-// commits them to the stage's `empty` mbarrier, which the builders wait on before
-// reusing the stage.  Every wait is bounded.
-// Epilogue: TMEM lane = component, column = pixel, so each tcgen05.ld row is one
-// component of 32 pixels and the planar output is written with coalesced stores.
+// samples.  Per K chunk of 32 samples, warps 0-14 (builders) form the KR rows of the
+// pass from the chunk's samples (prefetched into shared memory while the previous
+// chunk was built), expand the chunk's mask bits to bf16 and signal the stage's
+// `full` mbarrier; warp 15 waits on it, issues the MMAs (canonical K-major no-swizzle
+// layout: 8-row x 16-byte core matrices, LBO 128 B, SBO 512 B) and commits them to the
+// stage's `empty` mbarrier, which the builders wait on before reusing the stage.
+// Every wait is bounded.
+// Epilogue: TMEM lane = row, column = pixel, so each pair of tcgen05.ld rows gives the
+// (Re, Im) of one pair for 32 pixels, written as coalesced float2 stores.
 //
 // Output: planar per pixel, Cg[p][0 .. N^2): diagonal, then (Re, Im) per lower pair.
 #pragma once
@@ -39,7 +41,8 @@
 
 namespace dpl {
 
-constexpr int kTcM = 128;                    // components per M tile
+constexpr int kTcM = 128;                    // rows per M tile
+constexpr int kTcRows = 120;                 // rows of each M tile used per pass
 constexpr int kTcN = 256;                    // pixels per tile (MMA N)
 constexpr int kTcTileR = 16, kTcTileC = 16;  // tile of output pixels
 constexpr int kTcKC = 32;                    // samples per K chunk
@@ -53,7 +56,7 @@ struct TcArgs {
     int tiles_r, tiles_c;
     int region_r, region_c;  // max region extent of a tile
     int kpad, kwords;        // region samples padded to a multiple of kTcKC; 32-bit words per pixel
-    int npass;               // ceil(N^2 / 256)
+    int npass;               // 1 + ceil((N(N-1)/2 - (kTcRows - N)) / kTcRows)
     int ld_r;                // row stride of the per-pixel r = 1/sqrt(amp) table (odd)
     const cfloat* zt;        // (rows, cols, n) masked, pixel-major
     const uint32_t* bits;    // (out_rows, out_cols, wy, wpr) or null (rectangular window)
@@ -273,9 +276,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
         }
         __syncthreads();
         for (int pass = 0; pass < a.npass; ++pass) {
-            const int e0 = pass * 2 * kTcM;
-            const int e1 = min(e0 + 2 * kTcM, nn);
-            const int mt = e1 - e0 > kTcM ? 2 : 1;  // M tiles holding components
+            // rows of the pass: d0 diagonal rows (pass 0), then np lower pairs from qb on
+            const int d0 = pass == 0 ? n : 0;
+            const int qb = pass == 0 ? 0 : (kTcRows - n) + (pass - 1) * kTcRows;
+            const int np = max(min(O - qb, kTcRows - d0), 0);
+            const int rows0 = d0 + np;
+            const int mt = np > 0 ? 2 : 1;  // M tiles holding rows (tile 1: imaginary parts)
             if (builder) {
                 const int btid = tid;
                 if (!bulk) tc_prefetch(a, zbuf(0), soff, 0, btid);
@@ -301,41 +307,41 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                     if (*(volatile int*)sfail) break;
                     if (!bulk && ch + 1 < nchunks) tc_prefetch(a, zbuf(ch + 1), soff, ch + 1, btid);
                     const cfloat* zs = zbuf(ch);
-                    // one striped work list: KR items (component x 8 samples; consecutive
-                    // lanes take consecutive components, i.e. consecutive operand rows),
-                    // then mask items (pixel row x 16 samples)
-                    const int comps = e1 - e0, nkr = 4 * comps;
-                    for (int t = btid; t < nkr + 2 * kTcN; t += kTcBuilders) {
-                        if (t >= nkr) {
-                            const int m = t - nkr, row = m >> 1, half = m & 1;
-                            const uint32_t b = pbits[row * a.kwords + ch] >> (16 * half);
-                            *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(b);
-                            *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(b >> 8);
-                            continue;
-                        }
-                        const int g = (t >= comps) + (t >= 2 * comps) + (t >= 3 * comps), u = t - g * comps;
-                        const int kb = 8 * g, e = e0 + u;
+                    // Khatri-Rao items (row x 8 samples, at most one per builder; consecutive
+                    // lanes take consecutive rows), then mask items (pixel row x 16
+                    // samples), the latter starting on the builders without a row item
+                    const int nkr = 4 * rows0;
+                    if (btid < nkr) {
+                        const int g = (btid >= rows0) + (btid >= 2 * rows0) + (btid >= 3 * rows0);
+                        const int u = btid - g * rows0, kb = 8 * g;
                         const cfloat* zk = zs + kb * n;  // sample kb; + n per sample
-                        float x[8];
-                        if (e < n) {
-                            const cfloat* pi = zk + e;
+                        if (u < d0) {
+                            float x[8];
+                            const cfloat* pi = zk + u;
 #pragma unroll
                             for (int q = 0; q < 8; ++q, pi += n) x[q] = cabs2(*pi);
+                            tc_store8(stage, stage + 8192, u, kb, x);
                         } else {
-                            const uint32_t ij = pairs[(e - n) >> 1];
-                            const bool imag = (e - n) & 1;
+                            const uint32_t ij = pairs[qb + u - d0];
                             const cfloat* pi = zk + (ij & 0xffff);
                             const cfloat* pj = zk + (ij >> 16);
+                            float xr[8], xi[8];
 #pragma unroll
                             for (int q = 0; q < 8; ++q, pi += n, pj += n) {
                                 const cfloat zi = *pi, zj = *pj;
-                                const float re = fmaf(zi.re, zj.re, zi.im * zj.im);    // Re z_i conj(z_j)
-                                const float im = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
-                                x[q] = imag ? im : re;
+                                xr[q] = fmaf(zi.re, zj.re, zi.im * zj.im);     // Re z_i conj(z_j)
+                                xi[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
                             }
+                            tc_store8(stage, stage + 8192, u, kb, xr);
+                            tc_store8(stage + 16384, stage + 24576, u, kb, xi);
                         }
-                        unsigned char* hp = stage + (u >> 7) * 16384;
-                        tc_store8(hp, hp + 8192, u & 127, kb, x);
+                    }
+                    for (int m = (btid - nkr % kTcBuilders + kTcBuilders) % kTcBuilders; m < 2 * kTcN;
+                         m += kTcBuilders) {
+                        const int row = m >> 1, half = m & 1;
+                        const uint32_t bw = pbits[row * a.kwords + ch] >> (16 * half);
+                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(bw);
+                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(bw >> 8);
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
@@ -400,47 +406,67 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (*(volatile int*)sfail) break;
-            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (components) for the
-            // 32-pixel groups b = w / 4, w / 4 + 4, ... of each M tile
+            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) for the 16-pixel
+            // groups g = w / 4, w / 4 + 4, ... of both M tiles
             const int quarter = warp & 3;
             const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+            const int u = quarter * 32 + lane;  // this lane's row
             if (pass == 0) {
-                // the diagonal (|z_i|^2 sums) is components 0..n-1: r_i = 1 / sqrt(amp_i)
+                // the diagonal (|z_i|^2 sums) is rows 0..n-1 of M tile 0: r_i = 1 / sqrt(amp_i)
                 if (quarter * 32 < n) {
                     for (int g = warp >> 2; g < kTcN / 32; g += 4) {
                         uint32_t r[32];
                         tc_ld32(tmem + lane_base + (uint32_t)(32 * g), r);
-                        const int i = quarter * 32 + lane;
-                        if (i < n) {
+                        if (u < n) {
 #pragma unroll
                             for (int q = 0; q < 32; ++q)
-                                rtab[(32 * g + q) * a.ld_r + i] = 1.f / sqrtf(__uint_as_float(r[q]));
+                                rtab[(32 * g + q) * a.ld_r + u] = 1.f / sqrtf(__uint_as_float(r[q]));
                         }
                     }
                 }
                 __syncthreads();
             }
-            for (int b = warp >> 2; b < mt * (kTcN / 32); b += 4) {
-                const int t = b / (kTcN / 32), g = b % (kTcN / 32);
-                uint32_t r[32];
-                tc_ld32(tmem + lane_base + (uint32_t)(t * kTcN + 32 * g), r);
-                const int e = e0 + t * kTcM + quarter * 32 + lane;  // this lane's component
-                if (e < e1) {
-                    int ci = e, cj = e;
-                    if (e >= n) {
-                        const uint32_t ij = pairs[(e - n) >> 1];
-                        ci = ij & 0xffff;
-                        cj = ij >> 16;
-                    }
+            // (Re, Im) pairs go out as float2 where the planar rows keep 8-byte alignment
+            const bool v2 = (nn & 1) == 0 && (reinterpret_cast<uintptr_t>(a.Cg) & 7u) == 0;
+            if (quarter * 32 < rows0) {
+                for (int g = warp >> 2; g < kTcN / 16; g += 4) {  // 16-pixel groups
+                    uint32_t re[16], im[16];
+                    tc_ld16(tmem + lane_base + (uint32_t)(16 * g), re);
+                    if (mt == 2) tc_ld16(tmem + lane_base + (uint32_t)(kTcN + 16 * g), im);
+                    if (u < d0) {  // diagonal i = u
 #pragma unroll
-                    for (int q = 0; q < 32; ++q) {
-                        const int pl = 32 * g + q;
-                        const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
-                        if (pr < a.out_rows && pc < a.out_cols) {
-                            const float* rrow = rtab + pl * a.ld_r;
-                            const float f = rrow[ci] * rrow[cj];
-                            const int64_t p = (int64_t)pr * a.out_cols + pc;
-                            a.Cg[p * nn + e] = f < 1e6f ? __uint_as_float(r[q]) * f : 0.f;
+                        for (int q = 0; q < 16; ++q) {
+                            const int pl = 16 * g + q;
+                            const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
+                            if (pr < a.out_rows && pc < a.out_cols) {
+                                const float ri = rtab[pl * a.ld_r + u];
+                                const float f = ri * ri;
+                                const int64_t p = (int64_t)pr * a.out_cols + pc;
+                                a.Cg[p * nn + u] = f < 1e6f ? __uint_as_float(re[q]) * f : 0.f;
+                            }
+                        }
+                    } else if (u < rows0) {  // lower pair qb + u - d0
+                        const int o = qb + u - d0;
+                        const uint32_t ij = pairs[o];
+                        const int ci = ij & 0xffff, cj = ij >> 16, e = n + 2 * o;
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) {
+                            const int pl = 16 * g + q;
+                            const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
+                            if (pr < a.out_rows && pc < a.out_cols) {
+                                const float* rrow = rtab + pl * a.ld_r;
+                                const float f = rrow[ci] * rrow[cj];
+                                const bool ok = f < 1e6f;
+                                const float vr = ok ? __uint_as_float(re[q]) * f : 0.f;
+                                const float vi = ok ? __uint_as_float(im[q]) * f : 0.f;
+                                float* dst = a.Cg + ((int64_t)pr * a.out_cols + pc) * nn + e;
+                                if (v2) {
+                                    *reinterpret_cast<float2*>(dst) = make_float2(vr, vi);
+                                } else {
+                                    dst[0] = vr;
+                                    dst[1] = vi;
+                                }
+                            }
                         }
                     }
                 }

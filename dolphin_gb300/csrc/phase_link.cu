@@ -583,9 +583,10 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
     a.region_c = (kTcTileC - 1) * sx + wx;
     a.kpad = (int)(ceil_div((int64_t)a.region_r * a.region_c, kTcKC) * kTcKC);
     a.kwords = a.kpad / 32;
-    a.npass = ceil_div(n * n, 2 * kTcM);
     a.ld_r = n | 1;
     const int O = n * (n - 1) / 2;
+    // pass 0: the diagonal and kTcRows - n pairs; then kTcRows pairs per pass
+    a.npass = 1 + ceil_div(std::max(0, O - (kTcRows - n)), kTcRows);
     size_t o = 0;
     auto take = [&](size_t bytes, size_t al) {
         o = align_up(o, al);
@@ -801,15 +802,11 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
     return DPL_OK;
 }
 
-// Waits for `stream`, then reports what the enqueued pipeline left in the workspace: an
-// all-NaN SLC (the reference's message), an undefined PS brightness, a device timeout.
-static dpl_status pl_check(int n, const PlWorkspace& w, cudaStream_t s) {
-    int host_status[2] = {0, 0};
-    unsigned int host_valid[2] = {0, 0};
-    DPL_CUDA_TRY(cudaMemcpyAsync(host_status, w.status, sizeof(int), cudaMemcpyDeviceToHost, s));
-    DPL_CUDA_TRY(cudaMemcpyAsync(host_valid, w.valid_bits, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-    DPL_CUDA_TRY(cudaStreamSynchronize(s));
-    const unsigned long long vb = host_valid[0] | ((unsigned long long)host_valid[1] << 32);
+// Maps the status words the pipeline left (status, then the 64 per-SLC "has a finite
+// sample" bits) to the reference's errors: an all-NaN SLC (its message), an undefined
+// PS brightness, a device timeout.
+static dpl_status pl_decode(int n, const int* status, const unsigned int* valid) {
+    const unsigned long long vb = valid[0] | ((unsigned long long)valid[1] << 32);
     std::vector<int> bad;
     for (int t = 0; t < n; ++t)
         if (!((vb >> t) & 1ull)) bad.push_back(t);
@@ -820,10 +817,20 @@ static dpl_status pl_check(int n, const PlWorkspace& w, cudaStream_t s) {
         os << "]] out of " << n << " are all NaNs.";
         return fail(DPL_ERR_ALL_NAN_SLC, os.str());
     }
-    if (host_status[0] == DPL_ERR_INVALID_ARGUMENT)
+    if (status[0] == DPL_ERR_INVALID_ARGUMENT)
         return fail(DPL_ERR_INVALID_ARGUMENT, "a PS look window has no finite brightness (avg_mag is NaN at its PS pixels)");
-    if (host_status[0] != 0) return fail((dpl_status)host_status[0], "device-side error");
+    if (status[0] != 0) return fail((dpl_status)status[0], "device-side error");
     return DPL_OK;
+}
+
+// Waits for `stream`, then reports what the enqueued pipeline left in the workspace.
+static dpl_status pl_check(int n, const PlWorkspace& w, cudaStream_t s) {
+    int host_status[2] = {0, 0};
+    unsigned int host_valid[2] = {0, 0};
+    DPL_CUDA_TRY(cudaMemcpyAsync(host_status, w.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DPL_CUDA_TRY(cudaMemcpyAsync(host_valid, w.valid_bits, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    DPL_CUDA_TRY(cudaStreamSynchronize(s));
+    return pl_decode(n, host_status, host_valid);
 }
 
 extern "C" dpl_status dpl_phase_link(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
@@ -847,6 +854,26 @@ extern "C" dpl_status dpl_phase_link_status(const dpl_pl_params* prm, void* work
     pl_workspace_layout(prm->nslc, prm->rows, prm->cols, std::max(1, prm->sy), std::max(1, prm->sx), prm->cov_form,
                         (char*)workspace, &w);
     return pl_check((int)prm->nslc, w, (cudaStream_t)stream);
+}
+
+extern "C" dpl_status dpl_phase_link_status_copy(const dpl_pl_params* prm, void* workspace, size_t workspace_bytes,
+                                                 void* words, dpl_stream_t stream) {
+    if (!prm || !workspace || !words) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link_status_copy: null argument");
+    if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
+    PlWorkspace w;
+    pl_workspace_layout(prm->nslc, prm->rows, prm->cols, std::max(1, prm->sy), std::max(1, prm->sx), prm->cov_form,
+                        (char*)workspace, &w);
+    cudaStream_t s = (cudaStream_t)stream;
+    int* dst = static_cast<int*>(words);
+    DPL_CUDA_TRY(cudaMemcpyAsync(dst, w.status, sizeof(int), cudaMemcpyDefault, s));
+    DPL_CUDA_TRY(cudaMemcpyAsync(dst + 1, w.valid_bits, 2 * sizeof(unsigned int), cudaMemcpyDefault, s));
+    return DPL_OK;
+}
+
+extern "C" dpl_status dpl_phase_link_status_words(int64_t nslc, const void* words) {
+    if (!words) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link_status_words: null argument");
+    const int* w = static_cast<const int*>(words);
+    return pl_decode((int)nslc, w, reinterpret_cast<const unsigned int*>(w + 1));
 }
 
 extern "C" size_t dpl_covariance_workspace_size(int64_t nslc, int64_t rows, int64_t cols) {

@@ -8,7 +8,9 @@ exceptions.
 
 from __future__ import annotations
 
+import contextlib
 import math
+import threading
 from enum import IntEnum
 from typing import NamedTuple, Optional
 
@@ -22,6 +24,7 @@ __all__ = [
     "EstimatorType",
     "PhaseLinkOutput",
     "PhaseLinkRuntimeError",
+    "deferred_checks",
     "estimate_stack_covariance",
     "process_coherence_matrices",
     "run_phase_linking",
@@ -51,6 +54,35 @@ class PhaseLinkOutput(NamedTuple):
     estimator: object
     crlb_std_dev: object
     closure_phases: object
+
+
+_deferred = threading.local()
+
+
+@contextlib.contextmanager
+def deferred_checks():
+    """Defer the status checks of device-resident ``run_phase_linking`` calls.
+
+    Inside the block, a call on CUDA tensors enqueues its pipeline and a copy of its
+    three status words into pinned host memory, and returns without waiting for the
+    GPU, so that a block loop keeps the host ahead of the device.  On leaving the
+    block, each deferred status is waited for and checked in call order: the first
+    failure raises the exception that the synchronous call would have raised (e.g.
+    ``PhaseLinkRuntimeError`` for an all-NaN SLC).  The outputs of a failed call are
+    undefined.  Calls on host (numpy) arrays are not affected.  Not in the reference,
+    whose calls are synchronous.
+    """
+    prev = getattr(_deferred, "pending", None)
+    pending = []
+    _deferred.pending = pending
+    try:
+        yield
+    finally:
+        _deferred.pending = prev
+    lib = _lib.load()
+    for nslc, words, event in pending:
+        event.synchronize()
+        _lib.check(lib.dpl_phase_link_status_words(nslc, words.data_ptr()), "dpl_phase_link")
 
 
 def _is_complex(x) -> bool:
@@ -152,8 +184,20 @@ def run_phase_linking(
     outp = _lib.PlOutputs(cpx_phase=D.ptr(cpx), temp_coh=D.ptr(tcoh), shp_counts=D.ptr(counts),
                           eigenvalues=D.ptr(eig), estimator=D.ptr(est), crlb_std_dev=D.ptr(crlb),
                           closure_phases=D.ptr(clos) if nslc > 2 else None)
-    st = lib.dpl_phase_link(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle())
-    _lib.check(st, "dpl_phase_link")
+    pending = getattr(_deferred, "pending", None) if on_device else None
+    if pending is None:
+        st = lib.dpl_phase_link(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle())
+        _lib.check(st, "dpl_phase_link")
+    else:
+        torch = D.torch()
+        _lib.check(lib.dpl_phase_link_async(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle()),
+                   "dpl_phase_link_async")
+        words = torch.empty(3, dtype=torch.int32, pin_memory=True)
+        _lib.check(lib.dpl_phase_link_status_copy(prm, D.ptr(ws), ws.numel(), words.data_ptr(), D.stream_handle()),
+                   "dpl_phase_link_status_copy")
+        event = torch.cuda.Event()
+        event.record()
+        pending.append((nslc, words, event))
     if on_device:
         if counts is None:
             counts = D.require_cuda().zeros((out_rows, out_cols), dtype=D.torch().int16, device=cpx.device)

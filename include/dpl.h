@@ -160,6 +160,16 @@ dpl_status dpl_phase_link_async(const dpl_pl_params* params, const dpl_pl_inputs
 dpl_status dpl_phase_link_status(const dpl_pl_params* params, void* workspace,
                                  size_t workspace_bytes, dpl_stream_t stream);
 
+/* Deferred form of dpl_phase_link_status, for block loops that keep the host ahead of
+ * the GPU (no reference counterpart).  dpl_phase_link_status_copy enqueues on `stream`
+ * a copy of the call's three 32-bit status words from the workspace into `words`
+ * (pinned host or device memory, 12 bytes); the workspace may be reused once the copy
+ * has run.  After the caller has synchronised, dpl_phase_link_status_words maps the
+ * host copy to the status and message dpl_phase_link would have returned. */
+dpl_status dpl_phase_link_status_copy(const dpl_pl_params* params, void* workspace,
+                                      size_t workspace_bytes, void* words, dpl_stream_t stream);
+dpl_status dpl_phase_link_status_words(int64_t nslc, const void* words);
+
 /* ---------------------------------------------------------------------------------
  * Stage entry points (used to check each stage against the oracle).
  * ------------------------------------------------------------------------------- */

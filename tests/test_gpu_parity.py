@@ -351,6 +351,25 @@ def test_all_nan_slc_raises():
         dp.run_phase_linking(z, (2, 2))
 
 
+def test_deferred_checks_same_outputs_and_errors():
+    """Device calls inside deferred_checks() return the synchronous call's outputs, and
+    a failing call raises the synchronous call's exception when the block ends."""
+    z = torch.from_numpy(make_stack(StackConfig(nslc=8, rows=20, cols=22, seed=31, ps_frac=0.05))).cuda()
+    sync = [dp.run_phase_linking(z, (2, 3)), dp.run_phase_linking(z, (2, 3), use_evd=True)]
+    with dp.deferred_checks():
+        deferred = [dp.run_phase_linking(z, (2, 3)), dp.run_phase_linking(z, (2, 3), use_evd=True)]
+    for a, b in zip(sync, deferred):
+        for x, y in zip(a, b):
+            assert torch.equal(x, y)
+    bad = z.clone()
+    bad[2] = float("nan")
+    with pytest.raises(dp.PhaseLinkRuntimeError, match=r"slc_stack\[\[2\]\] out of 8 are all NaNs."):
+        with dp.deferred_checks():
+            dp.run_phase_linking(z, (2, 3))
+            dp.run_phase_linking(bad, (2, 3))  # returns; the error comes at the end of the block
+            dp.run_phase_linking(z, (2, 3))
+
+
 def test_mask_shape_and_dtype_errors():
     z = make_stack(StackConfig(nslc=5, rows=12, cols=12))
     with pytest.raises(ValueError, match="nodata_mask.shape"):
