@@ -75,6 +75,8 @@ extern "C" dpl_status dpl_compress(const float* slc, int64_t nslc, int64_t rows,
         return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_compress: reference_idx out of range");
     if (rows * cols == 0) return DPL_OK;
     if (!slc || !pl_cpx_phase || !comp_slc) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_compress: null pointer");
+    if (misaligned_c8(slc) || misaligned_c8(pl_cpx_phase) || misaligned_c8(comp_slc))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_compress: complex arrays must be 8-byte aligned");
     if (rows > INT32_MAX || cols > INT32_MAX) return fail(DPL_ERR_UNSUPPORTED, "dpl_compress: image too large");
     CompressArgs a{};
     a.n = (int)nslc;

@@ -58,9 +58,13 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
-struct cfloat {
+// interleaved complex64, 8-byte aligned so that one element is one 64-bit access
+struct __align__(8) cfloat {
     float re, im;
 };
+
+// complex arrays handed in through the C ABI must keep complex64's 8-byte alignment
+inline bool misaligned_c8(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) != 0; }
 
 __device__ __forceinline__ cfloat cmake(float r, float i) { return {r, i}; }
 __device__ __forceinline__ cfloat cadd(cfloat a, cfloat b) { return {a.re + b.re, a.im + b.im}; }

@@ -190,6 +190,8 @@ extern "C" dpl_status dpl_mlp_frame(const float* C, int nslc, int64_t npix, cons
     if (nslc < 1 || nslc > 64 || npix < 0) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_mlp_frame: bad shape");
     if (npix == 0) return DPL_OK;
     if (!C || !V || !out) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_mlp_frame: null pointer");
+    if (misaligned_c8(C) || misaligned_c8(V) || misaligned_c8(out))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_mlp_frame: complex arrays must be 8-byte aligned");
     const int64_t tot = npix * nslc;
     k_mlp_frame<<<(unsigned)ceil_div(tot, 256), 256, 0, (cudaStream_t)stream>>>(
         reinterpret_cast<const cfloat*>(C), nslc, npix, reinterpret_cast<const cfloat*>(V), conj_frame,

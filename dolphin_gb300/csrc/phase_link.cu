@@ -708,6 +708,10 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
     if (st != DPL_OK) return st;
     if (!in->slc || !out->cpx_phase || !out->temp_coh || !out->eigenvalues || !out->estimator || !out->crlb_std_dev)
         return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link: null array");
+    if (misaligned_c8(in->slc) || misaligned_c8(out->cpx_phase))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link: complex arrays must be 8-byte aligned");
+    if (reinterpret_cast<uintptr_t>(workspace) & 15u)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link: workspace must be 16-byte aligned");
     const int n = (int)P.nslc;
     const int ref = norm_ref(P.reference_idx, n);
     if (ref < 0 || ref >= n) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
@@ -894,6 +898,9 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
     if (cov_form != 0 && cov_form != 1)
         return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: cov_form must be 0 or 1 (2, fp64, is a phase-linking form)");
     if (!slc || !C || !workspace) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: null pointer");
+    if (misaligned_c8(slc) || misaligned_c8(C) || (reinterpret_cast<uintptr_t>(workspace) & 15u))
+        return fail(DPL_ERR_INVALID_ARGUMENT,
+                    "dpl_covariance: complex arrays must be 8-byte and the workspace 16-byte aligned");
     if (workspace_bytes < dpl_covariance_workspace_size(nslc, rows, cols))
         return fail(DPL_ERR_WORKSPACE, "dpl_covariance: workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
@@ -951,6 +958,8 @@ extern "C" dpl_status dpl_process_coherence(const float* C, int64_t npix, int ns
     if (npix == 0) return DPL_OK;
     if (!C || !eig_vecs || !eig_vals || !estimator || !crlb_std_dev || !temp_coh)
         return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence: null pointer");
+    if (misaligned_c8(C) || misaligned_c8(eig_vecs))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence: complex arrays must be 8-byte aligned");
     const int ref = norm_ref(reference_idx, nslc);
     if (ref < 0 || ref >= nslc) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
     PixArgs a{};
@@ -981,10 +990,14 @@ extern "C" dpl_status dpl_process_coherence_warm(const float* C, int64_t npix, i
     if (npix == 0) return DPL_OK;
     if (!C || !eig_vecs || !eig_vals || !estimator || !crlb_std_dev || !temp_coh)
         return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_warm: null pointer");
+    if (misaligned_c8(C) || misaligned_c8(eig_vecs))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_warm: complex arrays must be 8-byte aligned");
     const int ref = norm_ref(reference_idx, nslc);
     if (ref < 0 || ref >= nslc) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
     if (!workspace || workspace_bytes < dpl_process_coherence_workspace_size(npix))
         return fail(DPL_ERR_WORKSPACE, "dpl_process_coherence_warm: workspace too small");
+    if (vstart && misaligned_c8(vstart))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_warm: complex arrays must be 8-byte aligned");
     PixArgs a{};
     fill_pix_layout(a, nslc, 1);
     a.npix = npix;
@@ -1030,6 +1043,8 @@ extern "C" dpl_status dpl_process_coherence_noalloc(const float* C, int64_t npix
     if (npix == 0) return DPL_OK;
     if (!C || !eig_vecs || !eig_vals || !estimator || !crlb_std_dev || !temp_coh)
         return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_noalloc: null pointer");
+    if (misaligned_c8(C) || misaligned_c8(eig_vecs))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_process_coherence_noalloc: complex arrays must be 8-byte aligned");
     const int ref = norm_ref(reference_idx, nslc);
     if (ref < 0 || ref >= nslc) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
     int dev = 0;

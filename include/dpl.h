@@ -6,7 +6,9 @@
  * where noted).  No entry point allocates device memory: scratch space is passed
  * in by the caller (`workspace`, sized by the matching *_workspace_size call).
  * Arrays are C-contiguous; complex values are interleaved float pairs
- * (numpy complex64 layout); boolean arrays are one byte per element (0/1).
+ * (numpy complex64 layout, 8-byte aligned); boolean arrays are one byte per element
+ * (0/1).  Workspaces are 16-byte aligned (CUDA allocations are 256-byte aligned).
+ * A misaligned complex array or workspace is DPL_ERR_INVALID_ARGUMENT.
  *
  * Each function names the reference (dolphin) interface it replaces; paths are
  * relative to the dolphin source tree (src/dolphin/...).

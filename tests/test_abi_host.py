@@ -68,6 +68,34 @@ def test_invalid_arguments_fail_before_any_cuda_call(lib):
         _lib.check(st)
 
 
+def test_misaligned_complex_arrays_fail_before_any_cuda_call(lib):
+    """Complex arrays are read as 64-bit elements: a pointer that breaks complex64's
+    8-byte alignment (or a workspace off its 16-byte alignment) is refused up front."""
+    from dolphin_gb300 import _lib
+
+    odd, ok = 0x10004, 0x10000  # never dereferenced: the checks run before any launch
+    st = lib.dpl_compress(odd, 3, 4, 4, ok, 4, 4, 0, ok, 0, 0, ok, None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    assert b"8-byte aligned" in lib.dpl_last_error_message()
+    st = lib.dpl_mlp_frame(ok, 4, 10, odd, 0, ok, None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    prm = _lib.PlParams(nslc=5, rows=8, cols=8, hy=1, hx=1, sy=1, sx=1)
+    full = dict(cpx_phase=ok, temp_coh=ok, eigenvalues=ok, estimator=ok, crlb_std_dev=ok)
+    ws = lib.dpl_phase_link_workspace_size(prm)
+    st = lib.dpl_phase_link(prm, _lib.PlInputs(slc=odd), _lib.PlOutputs(**full), ok, ws, None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    st = lib.dpl_phase_link(prm, _lib.PlInputs(slc=ok), _lib.PlOutputs(**full), ok + 8, ws, None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    assert b"16-byte aligned" in lib.dpl_last_error_message()
+    st = lib.dpl_covariance(ok, 5, 8, 8, 1, 1, 1, 1, None, 0, odd, ok, 1 << 30, None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    st = lib.dpl_process_coherence(odd, 4, 5, 0, 0.0, 0.0, 0, 1.0, 0, 1, ok, ok, ok, ok, ok, None, ok, 1 << 30,
+                                   None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    with pytest.raises(ValueError, match="8-byte aligned"):
+        _lib.check(st)
+
+
 def test_workspace_sizes_are_positive(lib):
     from dolphin_gb300 import _lib
 
