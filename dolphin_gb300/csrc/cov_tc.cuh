@@ -16,21 +16,23 @@
 // diagonal; every other used row holds one lower pair, its real part in M tile 0 and
 // its imaginary part in the same row of M tile 1, so one builder thread forms both
 // from one pair of sample loads.  kTcRows = 120 rows per pass keep the Khatri-Rao work
-// of a K chunk at one item per builder thread.  The diagonal is in the first pass, so
-// every pass is normalised on the fly (covariance.py:131-142: C = numer /
-// sqrt(amp_i amp_j) where that is > 1e-6, evaluated as numer * r_i * r_j with
-// r = 1 / sqrt(amp), valid where r_i r_j < 1e6).
+// of a K chunk at one item per builder thread.  The kernel writes the sums unnormalised
+// (its shared memory goes to a third operand stage); the readers of the planar matrices
+// normalise them as covariance.py:131-142 does (C = numer / sqrt(amp_i amp_j) where that
+// is > 1e-6, evaluated as numer * r_i * r_j with r = 1 / sqrt(amp), and 0 where
+// r_i r_j >= 1e6).
 //
 // Per tile the masks are turned once into per-pixel bit arrays over the region's
 // samples.  Per K chunk of 32 samples, warps 0-14 (builders) form the KR rows of the
 // pass from the chunk's samples (prefetched into shared memory while the previous
 // chunk was built), expand the chunk's mask bits to bf16 and signal the stage's
-// `full` mbarrier; warp 15 waits on it, issues the MMAs (canonical K-major no-swizzle
+// `full` mbarrier (three operand stages where shared memory allows, else two); warp 15
+// waits on it, issues the MMAs (canonical K-major no-swizzle
 // layout: 8-row x 16-byte core matrices, LBO 128 B, SBO 512 B) and commits them to the
 // stage's `empty` mbarrier, which the builders wait on before reusing the stage.
 // Every wait is bounded.
 // Epilogue: TMEM lane = row, column = pixel, so each pair of tcgen05.ld rows gives the
-// (Re, Im) of one pair for 32 pixels, written as coalesced float2 stores.
+// (Re, Im) sums of one pair for 16 pixels, written as coalesced float2 stores.
 //
 // Output: planar per pixel, Cg[p][0 .. N^2): diagonal, then (Re, Im) per lower pair.
 #pragma once
@@ -50,6 +52,7 @@ constexpr int kTcThreads = 512;              // 16 warps
 constexpr int kTcBuilders = 480;             // warps 0-14; warp 15 issues the MMAs
 constexpr int kTcCols = 512;                 // TMEM columns: two M tiles x 256 pixels
 constexpr int kTcStageBytes = 4 * 8192 + 16384;  // KR hi/lo of two M tiles + mask
+constexpr int kTcMaxStages = 3;
 
 struct TcArgs {
     int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
@@ -57,7 +60,7 @@ struct TcArgs {
     int region_r, region_c;  // max region extent of a tile
     int kpad, kwords;        // region samples padded to a multiple of kTcKC; 32-bit words per pixel
     int npass;               // 1 + ceil((N(N-1)/2 - (kTcRows - N)) / kTcRows)
-    int ld_r;                // row stride of the per-pixel r = 1/sqrt(amp) table (odd)
+    int nst;                 // operand stages (2 or 3)
     const cfloat* zt;        // (rows, cols, n) masked, pixel-major
     const uint32_t* bits;    // (out_rows, out_cols, wy, wpr) or null (rectangular window)
     const uint8_t* nb_u8;    // alternative mask input (out_rows, out_cols, wy, wx)
@@ -66,7 +69,7 @@ struct TcArgs {
     int32_t* counts;         // (out_rows * out_cols) or null
     int* status;
     // shared-memory carve (bytes from the 1024-aligned base)
-    int off_stage, off_z, z_bytes, off_r, off_pbits, off_soff, off_runs, off_pair, off_bar, smem_bytes;
+    int off_stage, off_z, z_bytes, off_pbits, off_soff, off_runs, off_rows, off_bar, smem_bytes;
 };
 
 constexpr int kTcRuns = 3;  // contiguous runs of image samples per K chunk (a chunk spans <= 3 region rows)
@@ -98,13 +101,16 @@ __device__ __forceinline__ void tc_store8(unsigned char* hi_plane, unsigned char
     *reinterpret_cast<uint4*>(lo_plane + tc_off(row, kb)) = lw;
 }
 
-// 8 mask bits -> 8 bf16 (1.0 or 0), packed in pairs (bit 0 -> first element)
+// 8 mask bits -> 8 bf16 (1.0 or 0), packed in pairs (bit 0 -> first element): with
+// x = b | b << 15, bits 2k and 2k+1 of b sit at bits 0 and 16 of x >> 2k, and times
+// 0x3F80 (bf16 1.0) each becomes its 16-bit half
 __device__ __forceinline__ uint4 tc_expand8(uint32_t b) {
+    const uint32_t x = (b & 0xffu) | ((b & 0xffu) << 15);
     uint4 r;
-    r.x = ((b & 1u) ? 0x3F80u : 0u) | ((b & 2u) ? 0x3F800000u : 0u);
-    r.y = ((b & 4u) ? 0x3F80u : 0u) | ((b & 8u) ? 0x3F800000u : 0u);
-    r.z = ((b & 16u) ? 0x3F80u : 0u) | ((b & 32u) ? 0x3F800000u : 0u);
-    r.w = ((b & 64u) ? 0x3F80u : 0u) | ((b & 128u) ? 0x3F800000u : 0u);
+    r.x = (x & 0x10001u) * 0x3F80u;
+    r.y = ((x >> 2) & 0x10001u) * 0x3F80u;
+    r.z = ((x >> 4) & 0x10001u) * 0x3F80u;
+    r.w = ((x >> 6) & 0x10001u) * 0x3F80u;
     return r;
 }
 
@@ -163,29 +169,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n = a.n, nn = n * n, wy = 2 * a.hy + 1, wx = 2 * a.hx + 1;
     const int O = n * (n - 1) / 2;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [2] builders -> issuer
-    uint64_t* empty = full + 2;                                      // [2] MMAs done -> builders
-    uint64_t* zbar = full + 4;                                       // [kTcZBuf] bulk sample copies landed
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + a.off_bar + 64);
-    int* sfail = reinterpret_cast<int*>(sm + a.off_bar + 72);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [kTcMaxStages] builders -> issuer
+    uint64_t* empty = full + kTcMaxStages;                           // [kTcMaxStages] MMAs done -> builders
+    uint64_t* zbar = empty + kTcMaxStages;                           // [kTcZBuf] bulk sample copies landed
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(zbar + kTcZBuf);
+    int* sfail = reinterpret_cast<int*>(tmem_slot + 2);
     int2* runs = reinterpret_cast<int2*>(sm + a.off_runs);          // [nchunks][kTcRuns]
     const bool bulk = (a.n & 1) == 0;
     auto zbuf = [&](int c) { return reinterpret_cast<cfloat*>(sm + a.off_z + (c & (kTcZBuf - 1)) * a.z_bytes); };
-    float* rtab = reinterpret_cast<float*>(sm + a.off_r);             // [256][ld_r]: 1/sqrt(amp_i)
     uint32_t* pbits = reinterpret_cast<uint32_t*>(sm + a.off_pbits);  // [256][kwords]: pixel mask bits
     int* soff = reinterpret_cast<int*>(sm + a.off_soff);              // [kpad]: sample offsets in zt
-    uint32_t* pairs = reinterpret_cast<uint32_t*>(sm + a.off_pair);   // [O]: i | j << 16
+    // row table [npass][kTcRows]: i | j << 16 of the row's (i, j), i == j for the diagonal
+    uint32_t* rowtab = reinterpret_cast<uint32_t*>(sm + a.off_rows);
 
     for (int e = tid; e < kTcZBuf * a.z_bytes / 4; e += kTcThreads)  // no NaN patterns in unused slots
         reinterpret_cast<float*>(sm + a.off_z)[e] = 0.f;
-    for (int o = tid; o < O; o += kTcThreads) {
-        int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j, 0 <= j < i
-        while (i * (i - 1) / 2 > o) --i;
-        while ((i + 1) * i / 2 <= o) ++i;
-        pairs[o] = (uint32_t)i | ((uint32_t)(o - i * (i - 1) / 2) << 16);
+    for (int idx = tid; idx < a.npass * kTcRows; idx += kTcThreads) {
+        const int pass = idx / kTcRows, u = idx - pass * kTcRows;
+        const int d0 = pass == 0 ? n : 0;
+        const int o = (pass == 0 ? 0 : (kTcRows - n) + (pass - 1) * kTcRows) + u - d0;
+        uint32_t ij = 0u;  // unused rows: (0, 0)
+        if (u < d0) {
+            ij = (uint32_t)u | ((uint32_t)u << 16);
+        } else if (o < O) {
+            int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j, 0 <= j < i
+            while (i * (i - 1) / 2 > o) --i;
+            while ((i + 1) * i / 2 <= o) ++i;
+            ij = (uint32_t)i | ((uint32_t)(o - i * (i - 1) / 2) << 16);
+        }
+        rowtab[idx] = ij;
     }
     if (tid == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < a.nst; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&full[s])), "r"(kTcBuilders / 32));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&empty[s])), "r"(1));
         }
@@ -282,28 +297,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             const int np = max(min(O - qb, kTcRows - d0), 0);
             const int rows0 = d0 + np;
             const int mt = np > 0 ? 2 : 1;  // M tiles holding rows (tile 1: imaginary parts)
+            const uint32_t* rows_p = rowtab + pass * kTcRows;
             if (builder) {
                 const int btid = tid;
                 if (!bulk) tc_prefetch(a, zbuf(0), soff, 0, btid);
-                for (int ch = 0; ch < nchunks; ++ch) {
-                    const int s = ch & 1, zi = ch & (kTcZBuf - 1);
+                for (int ch = 0, s = 0; ch < nchunks; ++ch, s = s + 1 == a.nst ? 0 : s + 1) {
+                    const int zi = ch & (kTcZBuf - 1);
                     unsigned char* stage = sm + a.off_stage + s * kTcStageBytes;
                     unsigned char* msk = stage + 4 * 8192;
-                    // thread 0 waits until the MMAs that last read this stage are done and
-                    // (even N) the chunk's samples have landed; the named barrier then
-                    // releases every builder
+                    // Before building, the MMAs that last read this stage must be done and
+                    // the chunk's samples must have landed.  Even N (bulk copies): each
+                    // warp's lane 0 waits on the mbarriers and the warp reconverges, so the
+                    // warps run up to one chunk apart (a warp cannot wait on a phase more
+                    // than one ahead: the next one needs its own arrival on `full`).  Odd N
+                    // (cp.async by every builder): thread 0 waits, then the named barrier;
+                    // bar.sync counts a warp as arrived when any of its lanes arrives, so
+                    // warp 0 reconverges first.
+                    const bool waiter = bulk ? lane == 0 : btid == 0;
                     if ((pend >> s) & 1u) {
-                        if (btid == 0 && !tc_wait(&empty[s], (ph_empty >> s) & 1u)) atomicExch(sfail, 1);
+                        if (waiter && !tc_wait(&empty[s], (ph_empty >> s) & 1u)) atomicExch(sfail, 1);
                         ph_empty ^= 1u << s;
                         pend &= ~(1u << s);
                     }
                     if (bulk) {
-                        if (btid == 0 && !tc_wait(&zbar[zi], (ph_z >> zi) & 1u)) atomicExch(sfail, 1);
+                        if (waiter && !tc_wait(&zbar[zi], (ph_z >> zi) & 1u)) atomicExch(sfail, 1);
                         ph_z ^= 1u << zi;
+                        __syncwarp();
                     } else {
                         asm volatile("cp.async.wait_group 0;" ::: "memory");
+                        __syncwarp();
+                        asm volatile("bar.sync 1, %0;" ::"n"(kTcBuilders) : "memory");
                     }
-                    asm volatile("bar.sync 1, %0;" ::"n"(kTcBuilders) : "memory");
                     if (*(volatile int*)sfail) break;
                     if (!bulk && ch + 1 < nchunks) tc_prefetch(a, zbuf(ch + 1), soff, ch + 1, btid);
                     const cfloat* zs = zbuf(ch);
@@ -314,30 +338,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                     if (btid < nkr) {
                         const int g = (btid >= rows0) + (btid >= 2 * rows0) + (btid >= 3 * rows0);
                         const int u = btid - g * rows0, kb = 8 * g;
+                        const uint32_t ij = rows_p[u];
                         const cfloat* zk = zs + kb * n;  // sample kb; + n per sample
-                        if (u < d0) {
-                            float x[8];
-                            const cfloat* pi = zk + u;
+                        const cfloat* pi = zk + (ij & 0xffff);
+                        const cfloat* pj = zk + (ij >> 16);
+                        // Re and Im of z_i conj(z_j); for a diagonal row (i == j) Re = |z_i|^2
+                        // and the Im row (M tile 1) is not read back
+                        float xr[8], xi[8];
 #pragma unroll
-                            for (int q = 0; q < 8; ++q, pi += n) x[q] = cabs2(*pi);
-                            tc_store8(stage, stage + 8192, u, kb, x);
-                        } else {
-                            const uint32_t ij = pairs[qb + u - d0];
-                            const cfloat* pi = zk + (ij & 0xffff);
-                            const cfloat* pj = zk + (ij >> 16);
-                            float xr[8], xi[8];
-#pragma unroll
-                            for (int q = 0; q < 8; ++q, pi += n, pj += n) {
-                                const cfloat zi = *pi, zj = *pj;
-                                xr[q] = fmaf(zi.re, zj.re, zi.im * zj.im);     // Re z_i conj(z_j)
-                                xi[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));  // Im z_i conj(z_j)
-                            }
-                            tc_store8(stage, stage + 8192, u, kb, xr);
-                            tc_store8(stage + 16384, stage + 24576, u, kb, xi);
+                        for (int q = 0; q < 8; ++q) {
+                            const cfloat zi = pi[q * n], zj = pj[q * n];
+                            xr[q] = fmaf(zi.re, zj.re, zi.im * zj.im);
+                            xi[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));
                         }
+                        tc_store8(stage, stage + 8192, u, kb, xr);
+                        tc_store8(stage + 16384, stage + 24576, u, kb, xi);
                     }
-                    for (int m = (btid - nkr % kTcBuilders + kTcBuilders) % kTcBuilders; m < 2 * kTcN;
-                         m += kTcBuilders) {
+                    int m = btid - nkr;
+                    if (m < 0) m += kTcBuilders;
+                    for (; m < 2 * kTcN; m += kTcBuilders) {
                         const int row = m >> 1, half = m & 1;
                         const uint32_t bw = pbits[row * a.kwords + ch] >> (16 * half);
                         *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(bw);
@@ -352,7 +371,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                     pend |= 1u << s;
                 }
                 // drain: the last MMAs of the pass must be complete before the epilogue
-                for (int s2 = 0; s2 < 2; ++s2) {
+                for (int s2 = 0; s2 < a.nst; ++s2) {
                     if ((pend >> s2) & 1u) {
                         if (btid == 0 && !tc_wait(&empty[s2], (ph_empty >> s2) & 1u)) atomicExch(sfail, 1);
                         ph_empty ^= 1u << s2;
@@ -363,26 +382,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 // MMA issuer
                 constexpr uint32_t LBO = 128, SBO = kTcKC / 8 * 128;
                 const uint32_t idesc = tc_idesc_bf16(kTcM, kTcN);
+                // Descriptors of stage 0 (M tile 0, hi plane, k = 0) and of its mask.  Every
+                // other operand of a chunk lies a fixed offset away, and bits 0-13 of a
+                // descriptor hold the shared address >> 4: with every address below 256 KB,
+                // adding offset >> 4 never carries into the other fields.
+                const uint64_t dA = tc_desc(tc_smem(sm + a.off_stage), LBO, SBO);
+                const uint64_t dB = dA + (uint64_t)((4 * 8192) >> 4);
                 if (bulk)
                     for (int c = 0; c < kTcZBuf && c < nchunks; ++c) tc_prefetch_bulk(a, zbuf(c), &zbar[c], runs, c);
-                for (int ch = 0; ch < nchunks; ++ch) {
-                    const int s = ch & 1;
+                for (int ch = 0, s = 0; ch < nchunks; ++ch, s = s + 1 == a.nst ? 0 : s + 1) {
                     if (!tc_wait(&full[s], (ph_full >> s) & 1u)) {
                         atomicExch(sfail, 1);
                         break;
                     }
                     ph_full ^= 1u << s;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t st = tc_smem(sm + a.off_stage + s * kTcStageBytes);
-                    const uint32_t mk = st + 4 * 8192;
-                    for (int t = 0; t < mt; ++t) {
-                        const uint32_t khi = st + t * 16384, klo = khi + 8192;
+                    const uint64_t so = (uint64_t)((s * kTcStageBytes) >> 4);
+#pragma unroll
+                    for (int t = 0; t < 2; ++t) {
+                        if (t >= mt) break;
                         const uint32_t dt = tmem + (uint32_t)(t * kTcN);
+#pragma unroll
                         for (int kk = 0; kk < kTcKC; kk += 16) {
-                            const uint32_t koff = (kk / 8) * LBO;
-                            const uint64_t bd = tc_desc(mk + koff, LBO, SBO);
-                            const uint64_t ah = tc_desc(khi + koff, LBO, SBO);
-                            const uint64_t al = tc_desc(klo + koff, LBO, SBO);
+                            const uint64_t ko = (uint64_t)(((kk / 8) * LBO) >> 4);
+                            const uint64_t bd = dB + so + ko;
+                            const uint64_t ah = dA + so + (uint64_t)((t * 16384) >> 4) + ko;
+                            const uint64_t al = ah + (uint64_t)(8192 >> 4);
                             const uint32_t acc0 = (ch > 0 || kk > 0) ? 1u : 0u;
                             asm volatile(
                                 "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
@@ -411,60 +436,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             const int quarter = warp & 3;
             const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
             const int u = quarter * 32 + lane;  // this lane's row
-            if (pass == 0) {
-                // the diagonal (|z_i|^2 sums) is rows 0..n-1 of M tile 0: r_i = 1 / sqrt(amp_i)
-                if (quarter * 32 < n) {
-                    for (int g = warp >> 2; g < kTcN / 32; g += 4) {
-                        uint32_t r[32];
-                        tc_ld32(tmem + lane_base + (uint32_t)(32 * g), r);
-                        if (u < n) {
-#pragma unroll
-                            for (int q = 0; q < 32; ++q)
-                                rtab[(32 * g + q) * a.ld_r + u] = 1.f / sqrtf(__uint_as_float(r[q]));
-                        }
-                    }
-                }
-                __syncthreads();
-            }
             // (Re, Im) pairs go out as float2 where the planar rows keep 8-byte alignment
             const bool v2 = (nn & 1) == 0 && (reinterpret_cast<uintptr_t>(a.Cg) & 7u) == 0;
             if (quarter * 32 < rows0) {
-                for (int g = warp >> 2; g < kTcN / 16; g += 4) {  // 16-pixel groups
+                // this lane's row: its place in the planar output
+                const bool diag = u < d0;
+                const int e = diag ? u : n + 2 * (qb + u - d0);
+                // 16-pixel group g is row g of the 16 x 16 tile
+                const int qn = min(kTcTileC, a.out_cols - tc0);
+                for (int g = warp >> 2; g < kTcN / 16; g += 4) {
                     uint32_t re[16], im[16];
                     tc_ld16(tmem + lane_base + (uint32_t)(16 * g), re);
                     if (mt == 2) tc_ld16(tmem + lane_base + (uint32_t)(kTcN + 16 * g), im);
-                    if (u < d0) {  // diagonal i = u
+                    const int pr = tr0 + g;
+                    if (u < rows0 && pr < a.out_rows) {
+                        float* dst = a.Cg + ((int64_t)pr * a.out_cols + tc0) * nn + e;
 #pragma unroll
                         for (int q = 0; q < 16; ++q) {
-                            const int pl = 16 * g + q;
-                            const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
-                            if (pr < a.out_rows && pc < a.out_cols) {
-                                const float ri = rtab[pl * a.ld_r + u];
-                                const float f = ri * ri;
-                                const int64_t p = (int64_t)pr * a.out_cols + pc;
-                                a.Cg[p * nn + u] = f < 1e6f ? __uint_as_float(re[q]) * f : 0.f;
-                            }
-                        }
-                    } else if (u < rows0) {  // lower pair qb + u - d0
-                        const int o = qb + u - d0;
-                        const uint32_t ij = pairs[o];
-                        const int ci = ij & 0xffff, cj = ij >> 16, e = n + 2 * o;
-#pragma unroll
-                        for (int q = 0; q < 16; ++q) {
-                            const int pl = 16 * g + q;
-                            const int pr = tr0 + pl / kTcTileC, pc = tc0 + pl % kTcTileC;
-                            if (pr < a.out_rows && pc < a.out_cols) {
-                                const float* rrow = rtab + pl * a.ld_r;
-                                const float f = rrow[ci] * rrow[cj];
-                                const bool ok = f < 1e6f;
-                                const float vr = ok ? __uint_as_float(re[q]) * f : 0.f;
-                                const float vi = ok ? __uint_as_float(im[q]) * f : 0.f;
-                                float* dst = a.Cg + ((int64_t)pr * a.out_cols + pc) * nn + e;
-                                if (v2) {
-                                    *reinterpret_cast<float2*>(dst) = make_float2(vr, vi);
+                            if (q < qn) {
+                                if (diag) {
+                                    dst[(int64_t)q * nn] = __uint_as_float(re[q]);
+                                } else if (v2) {
+                                    *reinterpret_cast<float2*>(dst + (int64_t)q * nn) =
+                                        make_float2(__uint_as_float(re[q]), __uint_as_float(im[q]));
                                 } else {
-                                    dst[0] = vr;
-                                    dst[1] = vi;
+                                    dst[(int64_t)q * nn] = __uint_as_float(re[q]);
+                                    dst[(int64_t)q * nn + 1] = __uint_as_float(im[q]);
                                 }
                             }
                         }
@@ -481,7 +478,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     if (tid == 0 && *(volatile int*)sfail) atomicExch(a.status, (int)DPL_ERR_TIMEOUT);
     // before releasing TMEM make sure no MMA is still in flight (bounded)
     if (tid == 0)
-        for (int s2 = 0; s2 < 2; ++s2)
+        for (int s2 = 0; s2 < a.nst; ++s2)
             if ((pend >> s2) & 1u) tc_wait(&empty[s2], (ph_empty >> s2) & 1u);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();

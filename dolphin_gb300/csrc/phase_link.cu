@@ -291,12 +291,20 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
         if (MODE == kSolveOnly) {
             __syncwarp();
             if (a.Cplanar) {
+                // unnormalised planar sums: C_ij = numer_ij r_i r_j, r = 1 / sqrt(amp), 0 where
+                // r_i r_j >= 1e6 (covariance.py:131-142)
                 const float* src = a.Cplanar + p * n * n;
-                for (int i = 0; i < n; ++i)
+                for (int i = 0; i < n; ++i) {
+                    const float ri = __frsqrt_rn(src[i]);
                     for (int j = lane; j <= i; j += 32) {
+                        const float f = ri * __frsqrt_rn(src[j]);
+                        const bool ok = f < 1e6f;
                         const int o = i * (i - 1) / 2 + j;  // pair (i, j), i > j
-                        m.C[pk(i, j)] = i == j ? cmake(src[i], 0.f) : cmake(src[n + 2 * o], src[n + 2 * o + 1]);
+                        m.C[pk(i, j)] = i == j ? cmake(ok ? src[i] * f : 0.f, 0.f)
+                                               : (ok ? cmake(src[n + 2 * o] * f, src[n + 2 * o + 1] * f)
+                                                     : cmake(0.f, 0.f));
                     }
+                }
             } else {
                 const cfloat* src = a.Cin + p * n * n;
                 for (int i = 0; i < n; ++i)
@@ -326,7 +334,8 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
 
 namespace dpl {
 
-// planar coherence (tensor-core layout) -> full (npix, n, n) complex
+// planar sums (tensor-core layout) -> normalised full (npix, n, n) complex: C_ij =
+// numer_ij r_i r_j with r = 1 / sqrt(amp), 0 where r_i r_j >= 1e6 (covariance.py:131-142)
 __global__ void k_unpack_planar(const float* __restrict__ Cg, int n, int64_t npix, cfloat* __restrict__ out) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nn = (int64_t)n * n;
@@ -334,10 +343,16 @@ __global__ void k_unpack_planar(const float* __restrict__ Cg, int n, int64_t npi
     const int64_t p = e / nn;
     const int r = (int)(e - p * nn), i = r / n, j = r - i * n;
     const float* src = Cg + p * nn;
+    const int hi = i > j ? i : j, lo = i > j ? j : i;  // the stored pair (hi, lo)
+    const float f = __frsqrt_rn(src[hi]) * __frsqrt_rn(src[lo]);
+    const bool ok = f < 1e6f;
     cfloat v;
-    if (i == j) v = cmake(src[i], 0.f);
-    else if (i > j) v = cmake(src[n + 2 * (i * (i - 1) / 2 + j)], src[n + 2 * (i * (i - 1) / 2 + j) + 1]);
-    else v = cmake(src[n + 2 * (j * (j - 1) / 2 + i)], -src[n + 2 * (j * (j - 1) / 2 + i) + 1]);
+    if (i == j) {
+        v = cmake(ok ? src[i] * f : 0.f, 0.f);
+    } else {
+        const int o = n + 2 * (hi * (hi - 1) / 2 + lo);
+        v = ok ? cmake(src[o] * f, i > j ? src[o + 1] * f : -(src[o + 1] * f)) : cmake(0.f, 0.f);
+    }
     out[e] = v;
 }
 
@@ -583,28 +598,30 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
     a.region_c = (kTcTileC - 1) * sx + wx;
     a.kpad = (int)(ceil_div((int64_t)a.region_r * a.region_c, kTcKC) * kTcKC);
     a.kwords = a.kpad / 32;
-    a.ld_r = n | 1;
     const int O = n * (n - 1) / 2;
     // pass 0: the diagonal and kTcRows - n pairs; then kTcRows pairs per pass
     a.npass = 1 + ceil_div(std::max(0, O - (kTcRows - n)), kTcRows);
-    size_t o = 0;
-    auto take = [&](size_t bytes, size_t al) {
-        o = align_up(o, al);
-        size_t at = o;
-        o += bytes;
-        return (int)at;
-    };
-    a.off_stage = take(2 * (size_t)kTcStageBytes, 1024);
-    a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
-    a.off_z = take(kTcZBuf * (size_t)a.z_bytes, 16);
-    a.off_r = take((size_t)kTcN * a.ld_r * sizeof(float), 16);
-    a.off_pbits = take((size_t)kTcN * a.kwords * sizeof(uint32_t), 16);
-    a.off_soff = take((size_t)a.kpad * sizeof(int), 16);
-    a.off_runs = take((size_t)(a.kpad / kTcKC) * kTcRuns * sizeof(int2), 16);
-    a.off_pair = take((size_t)std::max(O, 1) * sizeof(uint32_t), 16);
-    a.off_bar = take(128, 64);
-    a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
-    return a.smem_bytes <= 227 * 1024;
+    // three operand stages where they fit in shared memory, else two
+    for (a.nst = kTcMaxStages; a.nst >= 2; --a.nst) {
+        size_t o = 0;
+        auto take = [&](size_t bytes, size_t al) {
+            o = align_up(o, al);
+            size_t at = o;
+            o += bytes;
+            return (int)at;
+        };
+        a.off_stage = take((size_t)a.nst * kTcStageBytes, 1024);
+        a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
+        a.off_z = take(kTcZBuf * (size_t)a.z_bytes, 16);
+        a.off_pbits = take((size_t)kTcN * a.kwords * sizeof(uint32_t), 16);
+        a.off_soff = take((size_t)a.kpad * sizeof(int), 16);
+        a.off_runs = take((size_t)(a.kpad / kTcKC) * kTcRuns * sizeof(int2), 16);
+        a.off_rows = take((size_t)a.npass * kTcRows * sizeof(uint32_t), 16);
+        a.off_bar = take(128, 64);
+        a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
+        if (a.smem_bytes <= 227 * 1024) break;
+    }
+    return a.nst >= 2 && a.smem_bytes <= 227 * 1024;
 }
 
 static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int sy, int sx, const cfloat* zt,

@@ -60,8 +60,8 @@ struct Grp {
     float* x;    // reduction slots (shared memory, 16 floats)
 
     __device__ __forceinline__ void sync() const {
-        if (G == 1) __syncwarp();
-        else asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(32 * G) : "memory");
+        __syncwarp();  // bar.sync counts a warp as arrived when any of its lanes arrives
+        if (G > 1) asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(32 * G) : "memory");
     }
     // sum over the group, the same value in every thread
     __device__ __forceinline__ float sum(float v) const {
@@ -435,11 +435,22 @@ __global__ void __launch_bounds__(256, 3 - G) k_solve_reg(PixArgs a, RegLayout L
             if (staged) asm volatile("cp.async.wait_group 0;" ::: "memory");
             gr.sync();
             const float* src = staged ? Gs : a.Cplanar + p * n * n;
-            if (me < n) Cf[me * ld + me] = cmake(src[me], 0.f);
+            // the planar sums are unnormalised: C_ij = numer_ij r_i r_j with r = 1 / sqrt(amp)
+            // (amp = the diagonal sum), 0 where r_i r_j >= 1e6 (covariance.py:131-142)
+            float* rv = reinterpret_cast<float*>(wb);
+            const float rme = me < n ? __frsqrt_rn(src[me]) : 0.f;
+            if (me < n) rv[me] = rme;
+            gr.sync();
+            if (me < n) {
+                const float f = rme * rme;
+                Cf[me * ld + me] = cmake(f < 1e6f ? src[me] * f : 0.f, 0.f);
+            }
             for (int i = 1; i < n; ++i) {
                 const int o = i * (i - 1) / 2;
                 if (me < i) {
-                    cfloat c = cmake(src[n + 2 * (o + me)], src[n + 2 * (o + me) + 1]);
+                    const float f = rv[i] * rme;
+                    cfloat c = f < 1e6f ? cmake(src[n + 2 * (o + me)] * f, src[n + 2 * (o + me) + 1] * f)
+                                        : cmake(0.f, 0.f);
                     if (lag > 0 && i - me >= lag) c = cmake(0.f, 0.f);
                     Cf[i * ld + me] = c;
                     Cf[me * ld + i] = cconj(c);

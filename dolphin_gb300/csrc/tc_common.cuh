@@ -51,7 +51,10 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
+// tcgen05.ld is warp-collective (.sync.aligned): the __syncwarp() reconverges a warp
+// whose lanes took different branches before the load
 __device__ __forceinline__ void tc_ld32(uint32_t addr, uint32_t (&r)[32]) {
+    __syncwarp();
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
         "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -65,6 +68,7 @@ __device__ __forceinline__ void tc_ld32(uint32_t addr, uint32_t (&r)[32]) {
 
 // the same for 16 columns
 __device__ __forceinline__ void tc_ld16(uint32_t addr, uint32_t (&r)[16]) {
+    __syncwarp();
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
