@@ -8,7 +8,7 @@
 
 namespace dpl {
 
-constexpr uint32_t kTcWaitLimit = 1u << 25;  // polls (>= 64 ns apart): a few seconds
+constexpr uint32_t kTcWaitLimit = 1u << 25;  // bound on the polls of a wait (>= 64 ns apart)
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = 0;
@@ -41,11 +41,24 @@ __device__ __forceinline__ bool tc_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// bounded wait with a short sleep between polls (a spinning thread would take issue
-// slots from the warps it waits for); returns false on timeout
+// the same with a suspend-time hint: the thread is suspended (taking no issue slots)
+// until the phase completes or about kTcSuspendNs have passed
+constexpr uint32_t kTcSuspendNs = 1000;
+__device__ __forceinline__ bool tc_try_wait_suspend(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(tc_smem(bar)), "r"(parity), "r"(kTcSuspendNs)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: suspended waits with a short sleep after each one that times out;
+// returns false after kTcWaitLimit / 8 of them (between ~0.3 and ~4 s)
 __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t it = 0; it < kTcWaitLimit; ++it) {
-        if (tc_try_wait(bar, parity)) return true;
+    for (uint32_t it = 0; it < kTcWaitLimit / 8; ++it) {
+        if (tc_try_wait_suspend(bar, parity)) return true;
         __nanosleep(64);
     }
     return false;
