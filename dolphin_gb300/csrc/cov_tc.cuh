@@ -15,7 +15,7 @@
 // (2 x 256 TMEM columns) row by row: in pass 0 rows 0 .. N-1 of M tile 0 hold the
 // diagonal; every other used row holds one lower pair, its real part in M tile 0 and
 // its imaginary part in the same row of M tile 1, so one builder thread forms both
-// from one pair of sample loads.  kTcRows = 120 rows per pass keep the Khatri-Rao work
+// from one pair of sample loads.  kTcRows = 128 rows per pass keep the Khatri-Rao work
 // of a K chunk at one item per builder thread.  The kernel writes the sums unnormalised
 // (its shared memory goes to a third operand stage); the readers of the planar matrices
 // normalise them as covariance.py:131-142 does (C = numer / sqrt(amp_i amp_j) where that
@@ -23,10 +23,10 @@
 // r_i r_j >= 1e6).
 //
 // Per tile the masks are turned once into per-pixel bit arrays over the region's
-// samples.  Per K chunk of 32 samples, warps 0-14 (builders) form the KR rows of the
+// samples.  Per K chunk of 32 samples, warps 0-16 (builders) form the KR rows of the
 // pass from the chunk's samples (prefetched into shared memory while the previous
 // chunk was built), expand the chunk's mask bits to bf16 and signal the stage's
-// `full` mbarrier (three operand stages where shared memory allows, else two); warp 15
+// `full` mbarrier (three operand stages where shared memory allows, else two); warp 17
 // waits on it, issues the MMAs (canonical K-major no-swizzle
 // layout: 8-row x 16-byte core matrices, LBO 128 B, SBO 512 B) and commits them to the
 // stage's `empty` mbarrier, which the builders wait on before reusing the stage.
@@ -44,12 +44,13 @@
 namespace dpl {
 
 constexpr int kTcM = 128;                    // rows per M tile
-constexpr int kTcRows = 120;                 // rows of each M tile used per pass
+constexpr int kTcRows = 128;                 // rows of each M tile used per pass
 constexpr int kTcN = 256;                    // pixels per tile (MMA N)
 constexpr int kTcTileR = 16, kTcTileC = 16;  // tile of output pixels
 constexpr int kTcKC = 32;                    // samples per K chunk
-constexpr int kTcThreads = 512;              // 16 warps
-constexpr int kTcBuilders = 480;             // warps 0-14; warp 15 issues the MMAs
+constexpr int kTcThreads = 576;              // 18 warps
+constexpr int kTcBuilders = 544;             // warps 0-16; warp 17 issues the MMAs
+static_assert(4 * kTcRows <= kTcBuilders, "one Khatri-Rao item per builder");
 constexpr int kTcCols = 512;                 // TMEM columns: two M tiles x 256 pixels
 constexpr int kTcStageBytes = 4 * 8192 + 16384;  // KR hi/lo of two M tiles + mask
 constexpr int kTcMaxStages = 3;
@@ -431,8 +432,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (*(volatile int*)sfail) break;
-            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) for the 16-pixel
-            // groups g = w / 4, w / 4 + 4, ... of both M tiles
+            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) for its share of
+            // the 16-pixel groups of both M tiles
             const int quarter = warp & 3;
             const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
             const int u = quarter * 32 + lane;  // this lane's row
@@ -444,7 +445,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 const int e = diag ? u : n + 2 * (qb + u - d0);
                 // 16-pixel group g is row g of the 16 x 16 tile
                 const int qn = min(kTcTileC, a.out_cols - tc0);
-                for (int g = warp >> 2; g < kTcN / 16; g += 4) {
+                // warps of this lane quarter: warp w takes groups w / 4, + nq, + 2 nq, ...
+                const int nq = (kTcThreads / 32 - quarter + 3) / 4;
+                for (int g = warp >> 2; g < kTcN / 16; g += nq) {
                     uint32_t re[16], im[16];
                     tc_ld16(tmem + lane_base + (uint32_t)(16 * g), re);
                     if (mt == 2) tc_ld16(tmem + lane_base + (uint32_t)(kTcN + 16 * g), im);
