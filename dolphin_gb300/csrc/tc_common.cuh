@@ -31,18 +31,8 @@ __device__ __forceinline__ uint32_t tc_idesc_bf16(int m, int nn) {
 
 __device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool tc_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(tc_smem(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// the same with a suspend-time hint: the thread is suspended (taking no issue slots)
-// until the phase completes or about kTcSuspendNs have passed
+// one test of an mbarrier phase with a suspend-time hint: the thread is suspended
+// (taking no issue slots) until the phase completes or about kTcSuspendNs have passed
 constexpr uint32_t kTcSuspendNs = 1000;
 __device__ __forceinline__ bool tc_try_wait_suspend(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
