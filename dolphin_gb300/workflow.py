@@ -43,7 +43,7 @@ from . import _device as D
 from . import _lib
 from ._types import HalfWindow, ShpMethod, Strides
 from .compress import compress
-from .phase_link import PhaseLinkRuntimeError, run_phase_linking
+from .phase_link import deferred_checks, run_phase_linking
 from .ps import calc_ps_block
 from .shp import estimate_neighbors
 from .similarity import stack_similarity
@@ -361,57 +361,78 @@ def run_wrapped_phase_single(slc_stack, *, half_window, strides=None, first_real
     eig = torch.zeros((orow, ocol), dtype=torch.float32, device=dev)
     est = torch.zeros((orow, ocol), dtype=torch.uint8, device=dev)
 
-    for out_b, trim, in_b, no_pad, in_trim in mgr.iter_blocks():
-        ir, ic = in_b
-        if bool(nodata[ir, ic].all()):
-            continue
-        cur = stack[:, ir, ic].contiguous()
-        if bool((cur == 0).all()) or bool(torch.isnan(cur).all()):
-            continue
-        amp_stack = cur.abs() if method == ShpMethod.KS else None
-        nb = estimate_neighbors(halfwin_rowcol=(hw.y, hw.x), alpha=shp_alpha, strides=st,
-                                mean=None if mean is None else mean[ir, ic].contiguous(),
-                                var=None if var is None else var[ir, ic].contiguous(),
-                                nslc=shp_nslc, amp_stack=amp_stack, method=method)
-        try:
-            out = run_phase_linking(cur, hw, st, use_evd=use_evd, beta=beta,
-                                    zero_correlation_threshold=zero_correlation_threshold,
-                                    reference_idx=output_reference_idx, nodata_mask=nodata[ir, ic].contiguous(),
-                                    ps_mask=psm[ir, ic].contiguous(), neighbor_arrays=nb, baseline_lag=baseline_lag,
-                                    avg_mag=None if mean is None else mean[ir, ic].contiguous(),
-                                    first_real_slc_idx=first_real_slc_idx, compute_crlb=write_crlb)
-        except PhaseLinkRuntimeError:
-            continue  # an all-NaN SLC in the block: the reference skips the block
-        cpx = torch.nan_to_num(out.cpx_phase)
-        blk_crlb = torch.nan_to_num(out.crlb_std_dev)
-        blk_tc = torch.nan_to_num(out.temp_coh)
-        tr, tc_ = trim
-        fr, fc = in_trim
-        inner = cur[:, fr, fc].contiguous()
-        bmean, bdisp, _ = calc_ps_block(inner[first_real_slc_idx:].abs().contiguous())
-        bcomp = compress(inner, cpx[:, tr, tc_].contiguous(), first_real_slc_idx=first_real_slc_idx, slc_mean=bmean,
-                         reference_idx=compressed_reference_idx)
-        o_r, o_c = out_b.row_start, out_b.col_start
-        part = cpx[first_real_slc_idx:, tr, tc_]
-        h, w = part.shape[-2:]
-        pl[:, o_r:o_r + h, o_c:o_c + w] = part
-        if crlb is not None:
-            crlb[:, o_r:o_r + h, o_c:o_c + w] = blk_crlb[first_real_slc_idx:, tr, tc_]
-        if clos is not None:
-            clos[o_r:o_r + h, o_c:o_c + w] = out.closure_phases[tr, tc_]
-        p_r, p_c = no_pad.row_start, no_pad.col_start
-        ch, cw = bcomp.shape
-        comp[p_r:p_r + ch, p_c:p_c + cw] = bcomp
-        disp[p_r:p_r + ch, p_c:p_c + cw] = bdisp
-        for dst, src, nd in ((tcoh, blk_tc, 0.0), (counts, out.shp_counts.to(torch.int32), 0.0),
-                             (eig, out.eigenvalues, 0.0), (est, out.estimator, 255.0)):
-            dst[o_r:o_r + h, o_c:o_c + w] = grow_nodata_region(src[tr, tc_].contiguous(), nodata=nd, n_pixels=2)
+    # The reference skips a block that is all nodata, all zero or all NaN, or that has an
+    # all-NaN SLC (run_phase_linking raises PhaseLinkRuntimeError, which the loop catches).
+    # Those decisions are taken for every block at once, with one read back to the host;
+    # the block loop then runs without a host synchronisation per block, its phase-linking
+    # status checks deferred to the end (any other error still raises).
+    blocks = list(mgr.iter_blocks())
+    checks = []
+    for _o, _t, (ir, ic), _n, _f in blocks:
+        cur = stack[:, ir, ic]
+        nan = torch.isnan(cur)
+        checks.append(torch.stack([nodata[ir, ic].all(), (cur == 0).all() | nan.all(),
+                                   nan.flatten(1).all(dim=1).any()]))
+    skip = torch.stack(checks).any(dim=1).tolist() if checks else []
+    with deferred_checks():
+        for (out_b, trim, in_b, no_pad, in_trim), skipped in zip(blocks, skip):
+            if not skipped:
+                _single_block(stack, out_b, trim, in_b, no_pad, in_trim, nodata, psm, mean, var, hw, st, method,
+                              shp_alpha, shp_nslc, use_evd, beta, zero_correlation_threshold, output_reference_idx,
+                              baseline_lag, first_real_slc_idx, write_crlb, compressed_reference_idx,
+                              (pl, crlb, clos, comp, disp, tcoh, counts, eig, est))
 
     sim = None
     if similarity:
         sim = stack_similarity(pl, search_radius=7, sim_type="median", nearest_n=similarity_nearest_n)
     # the shp_counts raster is uint16
     return SingleOutput(pl, crlb, clos, comp, disp, tcoh, counts.clamp(0, 65535).to(torch.uint16), eig, est, sim)
+
+
+def _single_block(stack, out_b, trim, in_b, no_pad, in_trim, nodata, psm, mean, var, hw, st, method, shp_alpha,
+                  shp_nslc, use_evd, beta, zero_correlation_threshold, output_reference_idx, baseline_lag,
+                  first_real_slc_idx, write_crlb, compressed_reference_idx, rasters):
+    """One block of the loop (workflows/single.py:215-294): SHPs, phase linking, the
+    compressed SLC, and the trimmed results written into the output rasters."""
+    torch = D.torch()
+    pl, crlb, clos, comp, disp, tcoh, counts, eig, est = rasters
+    ir, ic = in_b
+    cur = stack[:, ir, ic].contiguous()
+    amp_stack = cur.abs() if method == ShpMethod.KS else None
+    nb = estimate_neighbors(halfwin_rowcol=(hw.y, hw.x), alpha=shp_alpha, strides=st,
+                            mean=None if mean is None else mean[ir, ic].contiguous(),
+                            var=None if var is None else var[ir, ic].contiguous(),
+                            nslc=shp_nslc, amp_stack=amp_stack, method=method)
+    out = run_phase_linking(cur, hw, st, use_evd=use_evd, beta=beta,
+                            zero_correlation_threshold=zero_correlation_threshold,
+                            reference_idx=output_reference_idx, nodata_mask=nodata[ir, ic].contiguous(),
+                            ps_mask=psm[ir, ic].contiguous(), neighbor_arrays=nb, baseline_lag=baseline_lag,
+                            avg_mag=None if mean is None else mean[ir, ic].contiguous(),
+                            first_real_slc_idx=first_real_slc_idx, compute_crlb=write_crlb)
+    cpx = torch.nan_to_num(out.cpx_phase)
+    blk_crlb = torch.nan_to_num(out.crlb_std_dev)
+    blk_tc = torch.nan_to_num(out.temp_coh)
+    tr, tc_ = trim
+    fr, fc = in_trim
+    inner = cur[:, fr, fc].contiguous()
+    bmean, bdisp, _ = calc_ps_block(inner[first_real_slc_idx:].abs().contiguous())
+    bcomp = compress(inner, cpx[:, tr, tc_].contiguous(), first_real_slc_idx=first_real_slc_idx, slc_mean=bmean,
+                     reference_idx=compressed_reference_idx)
+    o_r, o_c = out_b.row_start, out_b.col_start
+    part = cpx[first_real_slc_idx:, tr, tc_]
+    h, w = part.shape[-2:]
+    pl[:, o_r:o_r + h, o_c:o_c + w] = part
+    if crlb is not None:
+        crlb[:, o_r:o_r + h, o_c:o_c + w] = blk_crlb[first_real_slc_idx:, tr, tc_]
+    if clos is not None:
+        clos[o_r:o_r + h, o_c:o_c + w] = out.closure_phases[tr, tc_]
+    p_r, p_c = no_pad.row_start, no_pad.col_start
+    ch, cw = bcomp.shape
+    comp[p_r:p_r + ch, p_c:p_c + cw] = bcomp
+    disp[p_r:p_r + ch, p_c:p_c + cw] = bdisp
+    for dst, src, nd in ((tcoh, blk_tc, 0.0), (counts, out.shp_counts.to(torch.int32), 0.0),
+                         (eig, out.eigenvalues, 0.0), (est, out.estimator, 255.0)):
+        dst[o_r:o_r + h, o_c:o_c + w] = grow_nodata_region(src[tr, tc_].contiguous(), nodata=nd, n_pixels=2)
 
 
 def _yx(v, cls):

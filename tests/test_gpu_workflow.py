@@ -177,3 +177,20 @@ def test_blocks_skipped_like_the_reference():
     assert (tc[25:35, 25:35] == 0).all()
     assert (_np(res.pl_slcs)[:, 1:13, 1:13] == 0).all()
     assert (tc[16:22, 16:22] > 0).all()
+
+
+def test_block_with_an_all_nan_slc_is_skipped():
+    """A block in which one SLC is entirely NaN makes run_phase_linking raise
+    PhaseLinkRuntimeError, and the reference's loop skips that block (its output stays 0);
+    the blocks around it are processed."""
+    cfg = StackConfig(nslc=5, rows=36, cols=36, seed=905, ps_frac=0.0)
+    z = make_stack(cfg)
+    # the block with output rows [25, 35) and columns [1, 13) reads rows [24, 36) and
+    # columns [0, 14): SLC 2 is NaN over all of it
+    z[2, 24:36, 0:14] = np.nan
+    res = W.run_wrapped_phase_single(z, half_window=(1, 1), block_shape=(12, 12), shp_method="rect")
+    tc = _np(res.temp_coh)
+    assert (tc[25:35, 1:13] == 0).all()
+    assert (_np(res.pl_slcs)[:, 25:35, 1:13] == 0).all()
+    assert (tc[25:35, 16:22] > 0).all()
+    assert (tc[16:22, 16:22] > 0).all()
