@@ -1,7 +1,6 @@
 """CPU-only checks: the C-ABI library loads and exports what include/dpl.h declares,
 argument validation maps to the reference's exceptions, and host-side logic."""
 
-import ctypes
 import re
 import types
 from pathlib import Path
