@@ -366,6 +366,12 @@ dpl_status dpl_process_coherence_noalloc(const float* C, int64_t npix, int nslc,
  * waiting for them to complete, then sets the enable state. */
 dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches);
 
+/* FP32 fused multiply-add throughput probe, the measured FP32 peak that the benchmark
+ * puts under the CUDA-core kernels' roofline (no reference counterpart).  Launches
+ * `blocks` x 256 threads, each running 8 independent chains of `iters` FMAs (16 * iters
+ * flop per thread), and writes one float per thread to `out` (blocks * 256 floats). */
+dpl_status dpl_fp32_fma_probe(float* out, int blocks, int iters, dpl_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
