@@ -167,3 +167,61 @@ def test_types_match_reference_field_order():
 
     assert HalfWindow(3, 5).y == 3 and Strides(2, 4).x == 4
     assert ShpMethod("glrt") is ShpMethod.GLRT and ShpMethod.NONE.value == "rect"
+
+
+def test_deferred_checks_bookkeeping(monkeypatch):
+    """deferred_checks() waits for and decodes every pending status in call order, raises
+    the first failure as the synchronous call would, and keeps nested blocks apart."""
+    from dolphin_gb300 import _lib
+    from dolphin_gb300 import phase_link as pl
+
+    log = []
+
+    class Event:
+        def __init__(self, tag):
+            self.tag = tag
+
+        def synchronize(self):
+            log.append(("wait", self.tag))
+
+    class Words:  # the "pointer" is the status the fake decoder returns
+        def __init__(self, status):
+            self.status = status
+
+        def data_ptr(self):
+            return self.status
+
+    class FakeLib:
+        def dpl_phase_link_status_words(self, nslc, words):
+            log.append(("decode", nslc))
+            return words
+
+        def dpl_last_error_message(self):
+            return b"slc_stack[[1]] out of 5 are all NaNs."
+
+    monkeypatch.setattr(_lib, "load", lambda path=None: FakeLib())
+    with pl.deferred_checks():
+        pl._deferred.pending.append((5, Words(_lib.DPL_OK), Event("a")))
+        with pl.deferred_checks():  # a nested block checks its own calls when it ends
+            pl._deferred.pending.append((7, Words(_lib.DPL_OK), Event("inner")))
+        assert log == [("wait", "inner"), ("decode", 7)]
+        pl._deferred.pending.append((6, Words(_lib.DPL_OK), Event("b")))
+    assert log[2:] == [("wait", "a"), ("decode", 5), ("wait", "b"), ("decode", 6)]
+    assert getattr(pl._deferred, "pending", None) is None
+
+    log.clear()
+    with pytest.raises(pl.PhaseLinkRuntimeError, match="are all NaNs"):
+        with pl.deferred_checks():
+            pl._deferred.pending.append((5, Words(_lib.DPL_OK), Event("ok")))
+            pl._deferred.pending.append((5, Words(_lib.DPL_ERR_ALL_NAN_SLC), Event("bad")))
+            pl._deferred.pending.append((5, Words(_lib.DPL_OK), Event("after")))
+    assert log == [("wait", "ok"), ("decode", 5), ("wait", "bad"), ("decode", 5)]
+    assert getattr(pl._deferred, "pending", None) is None
+
+    # an exception inside the block propagates without waiting on the pending calls
+    log.clear()
+    with pytest.raises(KeyError):
+        with pl.deferred_checks():
+            pl._deferred.pending.append((5, Words(_lib.DPL_OK), Event("x")))
+            raise KeyError("inside")
+    assert log == []
