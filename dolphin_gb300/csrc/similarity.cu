@@ -552,6 +552,8 @@ extern "C" dpl_status dpl_similarity_prep(const float* stack, int is_complex, in
     if (npix == 0) return DPL_OK;
     if (!valid || (m > 0 && !unit) || (nlayers > 0 && !stack))
         return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_similarity_prep: null pointer");
+    if ((is_complex && misaligned_c8(stack)) || misaligned_c8(unit))
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_similarity_prep: complex arrays must be 8-byte aligned");
     SimPrepArgs a{};
     a.nin = (int)nlayers;
     a.m = (int)m;
@@ -578,6 +580,8 @@ extern "C" dpl_status dpl_similarity(const float* unit, int64_t nlayers, int64_t
     const int64_t npix = rows * cols;
     if (npix == 0) return DPL_OK;
     if (!out || (nlayers > 0 && !unit)) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_similarity: null pointer");
+    if (misaligned_c8(unit))  // read with 8-byte cp.async copies
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_similarity: complex arrays must be 8-byte aligned");
     const int H = search_radius - 1;
     SimArgs a{};
     int K = 0, base[2 * kSimHMax + 1];

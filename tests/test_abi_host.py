@@ -93,6 +93,11 @@ def test_misaligned_complex_arrays_fail_before_any_cuda_call(lib):
     assert st == _lib.DPL_ERR_INVALID_ARGUMENT
     with pytest.raises(ValueError, match="8-byte aligned"):
         _lib.check(st)
+    st = lib.dpl_similarity_prep(odd, 1, 4, 8, 8, None, 0, ok, 4, ok, None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    st = lib.dpl_similarity(odd, 4, 8, 8, 3, 0, ok, None)
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    assert b"8-byte aligned" in lib.dpl_last_error_message()
 
 
 def test_workspace_sizes_are_positive(lib):
