@@ -52,6 +52,8 @@ __global__ void __launch_bounds__(256) k_grow_nodata(const T* in, T* out, int ro
 template <class T>
 static dpl_status grow_launch(const void* in, void* out, int64_t rows, int64_t cols, double nodata, int nan_nodata,
                               int n, cudaStream_t st) {
+    if (((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % alignof(T)) != 0)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_grow_nodata_region: arrays must be aligned to their element size");
     // the value written over grown pixels; where no pixel can be nodata (a NaN nodata
     // on integers, or a value the type cannot hold) it is never written
     T fill = T(0);

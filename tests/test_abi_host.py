@@ -98,6 +98,9 @@ def test_misaligned_complex_arrays_fail_before_any_cuda_call(lib):
     st = lib.dpl_similarity(odd, 4, 8, 8, 3, 0, ok, None)
     assert st == _lib.DPL_ERR_INVALID_ARGUMENT
     assert b"8-byte aligned" in lib.dpl_last_error_message()
+    st = lib.dpl_grow_nodata_region(ok + 2, ok, 0, 8, 8, 0.0, 0, 2, None)  # float32 at a 2-byte offset
+    assert st == _lib.DPL_ERR_INVALID_ARGUMENT
+    assert b"element size" in lib.dpl_last_error_message()
 
 
 def test_workspace_sizes_are_positive(lib):
