@@ -41,6 +41,10 @@ METRIC = "phase-linked pixels/sec (N=30, EMI) chosen vs plain GPU form at <=1e-3
 # workload, from an ncu capture (dram__bytes_read.sum 612,392,704 + dram__bytes_write.sum
 # 3,772,850,944); the planar coherence output (N^2 floats per pixel) is most of it
 COV_TC_TRAFFIC = 612_392_704 + 3_772_850_944
+# DRAM bytes (read + write) of one k_solve_reg launch on a 1034x1046-pixel block, scaled
+# from an ncu capture of the 778x790 block by the pixel count (the planar coherence read,
+# N^2 floats per pixel, is most of it); None until captured
+SOLVE_TRAFFIC = None
 UNIT = "pixels/s"
 
 
@@ -96,21 +100,48 @@ def cpu_sample(pool, cores, crop=(64, 128), repeats=1):
     return px / wall, desc
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def run_reference(args, rank, world):
+    """The CPU arm: the numpy restatement of the reference algorithm (the reference's own
+    path needs jax/numba, which neither machine has) on all host cores, each step a
+    bounded sample of the workload (16 crops of 64x128 output pixels plus halo, one
+    process per core)."""
     if rank != 0:
         return
     cores = len(os.sched_getaffinity(0))
     ctx = mp.get_context("spawn")
+    t_all = time.perf_counter()
     with ctx.Pool(cores) as pool:
         for _ in range(args.warmup):
             cpu_sample(pool, cores, crop=(16, 32))
-        vals = []
-        descs = []
+        vals, walls, descs = [], [], []
         for _ in range(args.steps):
+            t0 = time.perf_counter()
             v, d = cpu_sample(pool, cores)
+            walls.append(time.perf_counter() - t0)
             vals.append(v)
             descs.append(d)
+    wall_total = time.perf_counter() - t_all
     value = float(np.median(vals))
+    crops = cores
+    px_step = crops * 64 * 128
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -119,20 +150,86 @@ def run_reference(args, rank, world):
         "n_gpus": args.gpus,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1000.0 * FRAME * FRAME / value,
+        "ms_per_step": 1000.0 * float(np.median(walls)),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": f"N={NSLC} {FRAME}x{FRAME} stack, 1024x1024 blocks, half-window {HALF}, GLRT "
-                               f"{ALPHA}, EMI, PS {PS_THR} + fill, CRLB; bounded crops on CPU"},
+                               f"{ALPHA}, EMI, PS {PS_THR} + fill, CRLB; each step a bounded sample on the CPU: "
+                               f"{crops} crops of 64x128 output pixels (+halo) = {px_step} pixels",
+                   "pixels_per_step": px_step, "crops_per_step": crops,
+                   "warmup_sample": f"{crops} crops of 16x32 output pixels per warm-up step",
+                   "timed_wall_s": round(float(sum(walls)), 2), "run_wall_s": round(wall_total, 2),
+                   "projected_ms_per_frame": 1000.0 * FRAME * FRAME / value,
+                   "cpu_model": cpu_model()},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": descs[-1] + " (numpy restatement of the reference algorithm; the "
                                                "reference needs jax/numba, absent here)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _cpu_case_worker(args):
+    """One sub-crop of a CPU-table case, timed in its own process."""
+    kind, seed, nslc, out_rows, out_cols, half, use_evd, crlb = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    from dolphin_gb300.simulate import StackConfig, make_stack
+    from oracle import phase_link as O
+
+    hy, hx = half
+    cfg = StackConfig(nslc=nslc, rows=out_rows + 2 * hy, cols=out_cols + 2 * hx, seed=seed,
+                      ps_frac=0.03 if nslc == NSLC else 0.05)
+    z = make_stack(cfg)
+    t0 = time.perf_counter()
+    mean, disp, ps = O.calc_ps_block(np.abs(z), PS_THR, nslc)
+    if kind == "ps":
+        return out_rows * out_cols, time.perf_counter() - t0
+    nb = O.estimate_neighbors_glrt(mean, (disp * mean) ** 2, half, (1, 1), nslc, ALPHA)
+    O.run_phase_linking(z, half, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, use_evd=use_evd, compute_crlb=crlb)
+    return out_rows * out_cols, time.perf_counter() - t0
+
+
+def run_cpu_table(args):
+    """The CPU baseline table: the numpy restatement on all host cores, median of 3 timed
+    runs after one warm-up, for the 512x512 crop of the N=30 workload (EMI and EVD, CRLB on
+    and off), the whole N=10 128x128 configuration, and calc_ps_block alone.  Each run
+    splits its frame into one sub-crop (with halo) per core, one process each."""
+    cores = len(os.sched_getaffinity(0))
+    ctx = mp.get_context("spawn")
+    side = int(np.sqrt(cores))
+    while cores % side:
+        side -= 1
+    grid = (side, cores // side)
+    cases = [("config 2 crop 512x512, EMI, CRLB", "pl", NSLC, 512, HALF, False, True),
+             ("config 2 crop 512x512, EMI, no CRLB", "pl", NSLC, 512, HALF, False, False),
+             ("config 2 crop 512x512, EVD, CRLB", "pl", NSLC, 512, HALF, True, True),
+             ("config 1 128x128 (N=10, hw (5, 5)), EMI, CRLB", "pl", 10, 128, (5, 5), False, True),
+             ("calc_ps_block, config 2 crop 512x512", "ps", NSLC, 512, HALF, False, False)]
+    rows = []
+    with ctx.Pool(cores) as pool:
+        for name, kind, nslc, frame, half, evd, crlb in cases:
+            sub = (frame // grid[0], frame // grid[1])
+            jobs = [(kind, 20261205 + k, nslc, sub[0], sub[1], half, evd, crlb) for k in range(cores)]
+            walls = []
+            for rep in range(4):  # one warm-up, then three timed
+                t0 = time.perf_counter()
+                res = pool.map(_cpu_case_worker, jobs)
+                w = time.perf_counter() - t0
+                if rep:
+                    walls.append(w)
+            px = sum(r[0] for r in res)
+            med = float(np.median(walls))
+            rows.append({"run": name, "pixels": px, "median_wall_s": round(med, 3), "pixels_per_s": px / med,
+                         "walls_s": [round(w, 3) for w in walls]})
+            print(json.dumps(rows[-1]), flush=True)
+    print(json.dumps({"impl": "reference", "workload": "cpu-table", "cores": cores, "cpu_model": cpu_model(),
+                      "engine": "numpy restatement of the reference algorithm (oracle/phase_link.py), one "
+                                "process per core, OMP/OpenBLAS threads 1 per process",
+                      "grid": list(grid), "rows": rows}), flush=True)
 
 
 # ---------------------------------------------------------------------------------
@@ -195,9 +292,24 @@ def max_over_ranks(values, dist, device=None):
     return vals.tolist()
 
 
-def gpu_step(stack, plan, dp, outputs, covariance_form="tensor", use_evd=False):
-    """One pass of the hot path over every block of a device-resident stack."""
-    cpx_full, tc_full = outputs
+PL_FIELDS = ("cpx_phase", "temp_coh", "shp_counts", "eigenvalues", "estimator", "crlb_std_dev", "closure_phases")
+
+
+def frame_outputs(torch, frame, device=None, pin=False):
+    """Full-frame arrays for every PhaseLinkOutput field (device, or pinned host)."""
+    n = NSLC
+    spec = {"cpx_phase": ((n, frame, frame), torch.complex64), "temp_coh": ((frame, frame), torch.float32),
+            "shp_counts": ((frame, frame), torch.int32), "eigenvalues": ((frame, frame), torch.float32),
+            "estimator": ((frame, frame), torch.uint8), "crlb_std_dev": ((n, frame, frame), torch.float32),
+            "closure_phases": ((frame, frame, n - 2), torch.float32)}
+    if pin:
+        return {k: torch.empty(sh, dtype=dt, pin_memory=True) for k, (sh, dt) in spec.items()}
+    return {k: torch.empty(sh, dtype=dt, device=device) for k, (sh, dt) in spec.items()}
+
+
+def gpu_step(stack, plan, dp, outs, covariance_form="tensor", use_evd=False):
+    """One pass of the hot path over every block of a device-resident stack; every
+    output field of each block, trimmed to the block, goes into the frame arrays."""
     for (ir, ic, tr, tcl, orr, occ) in plan:
         blk = stack[:, ir[0]:ir[1], ic[0]:ic[1]].contiguous()
         mean, disp, ps = dp.calc_ps_block(blk.abs(), PS_THR, NSLC)
@@ -205,8 +317,11 @@ def gpu_step(stack, plan, dp, outputs, covariance_form="tensor", use_evd=False):
         nb = dp.estimate_neighbors(halfwin_rowcol=HALF, alpha=ALPHA, mean=mean, var=var, nslc=NSLC)
         out = dp.run_phase_linking(blk, HALF, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, compute_crlb=True,
                                    use_evd=use_evd, covariance_form=covariance_form)
-        cpx_full[:, orr[0]:orr[1], occ[0]:occ[1]] = out.cpx_phase[:, tr[0]:tr[1], tcl[0]:tcl[1]]
-        tc_full[orr[0]:orr[1], occ[0]:occ[1]] = out.temp_coh[tr[0]:tr[1], tcl[0]:tcl[1]]
+        src = (slice(tr[0], tr[1]), slice(tcl[0], tcl[1]))
+        dst = (slice(orr[0], orr[1]), slice(occ[0], occ[1]))
+        for k in PL_FIELDS:
+            lead = (slice(None),) if k in ("cpx_phase", "crlb_std_dev") else ()
+            outs[k][lead + dst] = getattr(out, k)[lead + src]
 
 
 def fp32_peak_tflops(torch, lib, dev):
@@ -271,12 +386,11 @@ def run_ours(args, rank, world, pool, cores):
     cfg = StackConfig(nslc=NSLC, rows=frame, cols=frame, seed=SEED + rank, ps_frac=0.03)
     stack = make_stack_torch(cfg, device=dev)
     plan = block_plan(frame, frame, BLOCK, HALF)
-    cpx_full = torch.empty((NSLC, frame, frame), dtype=torch.complex64, device=dev)
-    tc_full = torch.empty((frame, frame), dtype=torch.float32, device=dev)
+    outs = frame_outputs(torch, frame, dev)
     lib = _lib.load()
 
     for _ in range(args.warmup):
-        gpu_step(stack, plan, dp, (cpx_full, tc_full))
+        gpu_step(stack, plan, dp, outs)
     torch.cuda.synchronize()
 
     # ---- device-resident timed region ----
@@ -294,7 +408,7 @@ def run_ours(args, rank, world, pool, cores):
     # instead of one host synchronisation per block
     with dp.deferred_checks():
         for _ in range(args.steps):
-            gpu_step(stack, plan, dp, (cpx_full, tc_full))
+            gpu_step(stack, plan, dp, outs)
         e1.record()
     torch.cuda.synchronize()
     barrier()
@@ -308,15 +422,15 @@ def run_ours(args, rank, world, pool, cores):
     # ---- the same stack through the plain GPU form (SIMT covariance fused with the
     # solver) and through EVD, on the first two blocks ----
     sub = plan[:2]
-    plain_rate = form_rate(torch, stack, sub, dp, (cpx_full, tc_full), covariance_form="simt")
-    chosen_rate = form_rate(torch, stack, sub, dp, (cpx_full, tc_full))
-    evd_rate = form_rate(torch, stack, sub, dp, (cpx_full, tc_full), use_evd=True)
+    plain_rate = form_rate(torch, stack, sub, dp, outs, covariance_form="simt")
+    chosen_rate = form_rate(torch, stack, sub, dp, outs)
+    evd_rate = form_rate(torch, stack, sub, dp, outs, use_evd=True)
+    accuracy = fp64_check(torch, dp, stack, plan[0])
 
-    # ---- end-to-end: pinned host stack in, host results out, through the public API ----
+    # ---- end-to-end: pinned host stack in, every output field out, through the public API ----
     host_stack = torch.empty(stack.shape, dtype=stack.dtype, pin_memory=True)
     host_stack.copy_(stack)
-    host_cpx = torch.empty(cpx_full.shape, dtype=cpx_full.dtype, pin_memory=True)
-    host_tc = torch.empty(tc_full.shape, dtype=tc_full.dtype, pin_memory=True)
+    host_outs = frame_outputs(torch, frame, pin=True)
     del stack
     torch.cuda.empty_cache()
     dstack = torch.empty(host_stack.shape, dtype=host_stack.dtype, device=dev)
@@ -351,15 +465,18 @@ def run_ours(args, rank, world, pool, cores):
             comp.wait_event(ev)
             if out_done[r] is not None:
                 comp.wait_event(out_done[r])
-            gpu_step(dstack, [e for e in plan if e[4] == (r0, r1)], dp, (cpx_full, tc_full))
+            gpu_step(dstack, [e for e in plan if e[4] == (r0, r1)], dp, outs)
             done = torch.cuda.Event()
             done.record(comp)
             comp_done[r] = done
             with torch.cuda.stream(copy_out):
                 copy_out.wait_event(done)
-                for t in range(NSLC):
-                    host_cpx[t, r0:r1].copy_(cpx_full[t, r0:r1], non_blocking=True)
-                host_tc[r0:r1].copy_(tc_full[r0:r1], non_blocking=True)
+                for k in PL_FIELDS:  # every output; contiguous slabs of pinned memory
+                    if k in ("cpx_phase", "crlb_std_dev"):
+                        for t in range(NSLC):
+                            host_outs[k][t, r0:r1].copy_(outs[k][t, r0:r1], non_blocking=True)
+                    else:
+                        host_outs[k][r0:r1].copy_(outs[k][r0:r1], non_blocking=True)
                 od = torch.cuda.Event()
                 od.record(copy_out)
                 out_done[r] = od
@@ -381,37 +498,38 @@ def run_ours(args, rank, world, pool, cores):
     barrier()
     e2e_ms = f0.elapsed_time(f1) / e2e_steps
     h2d = sum((b1 - b0) for (b0, b1) in bands) * NSLC * frame * host_stack.element_size()
-    d2h = host_cpx.numel() * host_cpx.element_size() + host_tc.numel() * host_tc.element_size()
+    d2h = sum(v.numel() * v.element_size() for v in host_outs.values())
 
     ms, e2e_ms, cov_ms, sol_ms = max_over_ranks([ms, e2e_ms, cov_ms, sol_ms], dist, dev)
     if rank != 0:
         return
     px = frame * frame * world
     value = px / (ms / 1000.0)
-    # roofline of the covariance contraction (tensor cores): algorithmic flops
-    # F_cov = 4 W N (N + 1) per output pixel (Hermitian half, complex MAC = 8 flops)
-    W = (2 * HALF[0] + 1) * (2 * HALF[1] + 1)
-    f_cov = 4.0 * W * NSLC * (NSLC + 1)
     px_per_launch = sum((ir[1] - ir[0]) * (ic[1] - ic[0]) for (ir, ic, *_r) in plan) / len(plan)
-    achieved = f_cov * px_per_launch / (cov_ms / 1000.0) / 1e12
-    # solver flops per pixel (EMI): Cholesky + inverse of |Gamma| (~N^3), complex
-    # Cholesky of A - 0.99 I (4N^3/3), ~7 inverse iterations (8N^2 each), CRLB (~2N^3/3)
+    # solver flops per pixel (EMI), the dominant kernel: Cholesky + inverse of |Gamma|
+    # (~N^3), complex Cholesky of A - 0.99 I (4N^3/3), ~7 inverse iterations (8N^2 each),
+    # CRLB (~2N^3/3)
     f_sol = NSLC**3 * (1.0 + 4.0 / 3.0 + 2.0 / 3.0) + 7 * 8.0 * NSLC**2
     fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
     fp32_peak = fp32_peak_tflops(torch, lib, dev)
-    ach_sol = f_sol * px_per_launch / (sol_ms / 1000.0) / 1e12 if sol_ms > 0 else None
+    ach_sol = f_sol * px_per_launch / (sol_ms / 1000.0) / 1e12
+    # covariance contraction (tensor cores): F_cov = 4 W N (N + 1) per output pixel
+    # (Hermitian half, complex MAC = 8 flops)
+    W = (2 * HALF[0] + 1) * (2 * HALF[1] + 1)
+    f_cov = 4.0 * W * NSLC * (NSLC + 1)
+    ach_cov = f_cov * px_per_launch / (cov_ms / 1000.0) / 1e12
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
     except (OSError, ValueError):
         pass
-    peak = float(peaks.get("bf16_tflops", 1900.0))
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
     cpu = None
     if pool is not None:
         cv, cd = cpu_sample(pool, cores)
         cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": cd + " (numpy restatement of the reference algorithm)"}
-    # per block: k_ps_block, k_glrt_scale, k_glrt, k_prep, k_cov_tc, k_pixel (solve), k_pixel (LU list), k_post
+    # per block: k_ps_block, k_glrt_scale, k_glrt, k_prep, k_cov_tc, k_solve_reg, k_pixel (LU list), k_post
     launches_per_step = len(plan) * 8
     line = {
         "metric": METRIC,
@@ -432,20 +550,23 @@ def run_ours(args, rank, world, pool, cores):
                    "form": "chosen: tensor-core covariance (bf16 hi/lo, fp32 accumulate) + FP32 solver",
                    "status_checks": "every block's status copied back and checked at the end of the timed "
                                     "region (deferred_checks), no host synchronisation per block",
-                   "e2e_copies": "pinned host stack in by row band, results out by block row, overlapping "
-                                 "compute within and across steps"},
+                   "e2e_copies": "pinned host stack in by row band, all seven PhaseLinkOutput fields out by "
+                                 "block row, overlapping compute within and across steps"},
         "e2e": {"value": px / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_per_step * args.steps),
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": COV_TC_TRAFFIC if frame == FRAME else None,
-                     "kernel": "k_cov_tc", "kernel_ms": cov_ms, "launches_per_step": launches_cov,
-                     "note": "algorithmic covariance flops 4*W*N*(N+1) per pixel over the measured launch time "
-                             "(CUDA events on the launch stream); peak = measured bf16 dense (of measured)"},
-        "solver": {"kernel": "k_solve_reg (register solver)", "kernel_ms": sol_ms,
-                   "achieved_tflops": ach_sol, "fp32_peak_tflops": fp32_peak,
-                   "frac": ach_sol / fp32_peak if ach_sol else None, "fp32_nominal_tflops": fp32_nominal,
-                   "note": "FP32 CUDA-core bound; algorithmic flops ~(3N^3 + 56N^2) per pixel; peak measured on "
-                           "this GPU with dpl_fp32_fma_probe (of measured), nominal beside it"},
+        "roofline": {"bound": "fp32", "achieved": ach_sol, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": ach_sol / fp32_peak, "traffic": SOLVE_TRAFFIC if frame == FRAME else None,
+                     "kernel": "k_solve_reg", "kernel_ms": sol_ms, "launches_per_step": cnt[1] / args.steps,
+                     "fp32_nominal_tflops": fp32_nominal,
+                     "note": "dominant kernel (FP32 CUDA cores): algorithmic flops ~(3N^3 + 56N^2) per pixel over "
+                             "the CUDA-event launch time on its stream; peak = FP32 FMA rate measured on this GPU "
+                             "with dpl_fp32_fma_probe (of measured)"},
+        "roofline_covariance": {"bound": "tensor", "achieved": ach_cov, "peak": bf16_peak, "unit": "TFLOP/s",
+                                "frac": ach_cov / bf16_peak, "traffic": COV_TC_TRAFFIC if frame == FRAME else None,
+                                "kernel": "k_cov_tc", "kernel_ms": cov_ms, "launches_per_step": launches_cov,
+                                "note": "algorithmic covariance flops 4*W*N*(N+1) per pixel; peak = measured bf16 "
+                                        "dense (of measured)"},
+        "accuracy_vs_fp64": accuracy,
         "clocks": clocks,
         "forms": {"blocks": len(sub), "unit": UNIT, "chosen": chosen_rate, "plain": plain_rate,
                   "chosen_over_plain": chosen_rate / plain_rate, "evd_chosen": evd_rate,
@@ -455,6 +576,45 @@ def run_ours(args, rank, world, pool, cores):
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+
+
+def block_inputs(dp, stack, entry):
+    """PS and GLRT inputs of one block of the plan (as gpu_step makes them)."""
+    ir, ic = entry[0], entry[1]
+    blk = stack[:, ir[0]:ir[1], ic[0]:ic[1]].contiguous()
+    mean, disp, ps = dp.calc_ps_block(blk.abs(), PS_THR, NSLC)
+    nb = dp.estimate_neighbors(halfwin_rowcol=HALF, alpha=ALPHA, mean=mean, var=(disp * mean) ** 2, nslc=NSLC)
+    return blk, mean, disp, ps, nb
+
+
+def compare_to_fp64(torch, out, ref, ps):
+    """Errors of a float32 run against the FP64 form on one block: phase (per pixel, the
+    worst SLC) and temporal coherence where the FP64 coherence is above 0.3; EMI/EVD
+    flips and where they fall."""
+    good = ref.temp_coh > 0.3
+    d = torch.angle(out.cpx_phase * ref.cpx_phase.conj()).abs().amax(0)
+    t = (out.temp_coh - ref.temp_coh).abs()
+    flip = out.estimator != ref.estimator
+    psm = ps.bool()
+    dg = d[good]
+    return {"pixels": int(d.numel()), "coherent": int(good.sum()), "phase_max_rad": float(dg.max()),
+            "phase_p99_rad": float(torch.quantile(dg[:2**24].float(), 0.99)),
+            "above_1e-3_rad": int((dg > 1e-3).sum()), "temp_coh_max": float(t[good].max()),
+            "flips": int(flip.sum()), "flips_on_ps": int((flip & psm).sum()),
+            "flips_fp64_emi": int((flip & (ref.estimator == 1)).sum()),
+            "flips_phase_max_rad": float(d[flip & good].max()) if (flip & good).any() else 0.0}
+
+
+def fp64_check(torch, dp, stack, entry):
+    """The chosen form against the FP64 GPU form (covariance and solver in double) on
+    one 1034x1046 block of the workload."""
+    blk, mean, _disp, ps, nb = block_inputs(dp, stack, entry)
+    kw = dict(ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, compute_crlb=True)
+    out = dp.run_phase_linking(blk, HALF, **kw)
+    ref = dp.run_phase_linking(blk, HALF, covariance_form="fp64", **kw)
+    r = compare_to_fp64(torch, out, ref, ps)
+    r["block"] = [list(entry[0]), list(entry[1])]
+    return r
 
 
 def run_precision(args):
@@ -520,6 +680,174 @@ def run_precision(args):
                       "fp64_crop": {"pixels": int(crop.shape[1] * crop.shape[2]), "rates": crop_rates,
                                     "coherent_pixels": int(good.sum()), "errors_vs_fp64": errs}}),
           flush=True)
+
+
+def glrt_check(torch, mean, disp, nb, nslc, alpha, rows_per_chunk=64):
+    """GLRT masks of one block against the float64 statistic: every test evaluated as
+    nslc * log1p((s1 - s2)^2 / (4 s1 s2)) in float64 on the float32 scale^2, with the
+    reference's window rules (clamped start, validity from the unclamped origin, centre
+    excluded).  Returns (tests, tests within 1e-6 relative of the cutoff, masks that
+    differ from the float64 decision)."""
+    from scipy import stats
+
+    rows, cols = mean.shape
+    hy, hx = HALF
+    wy, wx = 2 * hy + 1, 2 * hx + 1
+    scale2 = ((disp * mean) ** 2 + mean * mean) / 2  # float32, as the kernels compute it
+    s64 = scale2.double()
+    thr = float(np.float32(stats.chi2.ppf(1 - alpha, df=1)))
+    dev = mean.device
+    r_idx = torch.arange(rows, device=dev)
+    c_idx = torch.arange(cols, device=dev)
+    c0 = (c_idx - hx).clamp(min=0).clamp(max=cols - wx)
+    wb = torch.arange(wx, device=dev)
+    wa = torch.arange(wy, device=dev)
+    cc = c0[:, None] + wb[None, :]  # (cols, wx)
+    valid_c = ((c_idx[:, None] - hx + wb[None, :]) >= 0) & ((c_idx[:, None] - hx + wb[None, :]) < cols)
+    tests = near = differ = 0
+    for r_start in range(0, rows, rows_per_chunk):
+        rr = r_idx[r_start:r_start + rows_per_chunk]
+        r0 = (rr - hy).clamp(min=0).clamp(max=rows - wy)
+        ri = r0[:, None] + wa[None, :]  # (R, wy)
+        valid_r = ((rr[:, None] - hy + wa[None, :]) >= 0) & ((rr[:, None] - hy + wa[None, :]) < rows)
+        s2 = s64[ri[:, None, :, None], cc[None, :, None, :]]  # (R, C, wy, wx)
+        s1 = s64[rr][:, :, None, None]
+        t = float(nslc) * torch.log1p((s1 - s2) ** 2 / (4.0 * s1 * s2))
+        valid = valid_r[:, None, :, None] & valid_c[None, :, None, :]
+        valid[:, :, hy, hx] = False
+        want = (thr > t) & valid
+        got = nb[r_start:r_start + rows_per_chunk].bool()
+        tests += int(valid.sum())
+        near += int(((t - thr).abs() <= 1e-6 * thr)[valid].sum())
+        differ += int((got != want).sum())
+    return tests, near, differ
+
+
+def run_parity(args):
+    """The chosen form against the FP64 GPU form over the whole N=30 frame, block by block
+    (the FP64 form computes the covariance and the solve in double); GLRT masks against
+    the float64 statistic; near-cutoff counts for the GLRT and PS tests."""
+    import torch
+
+    import dolphin_gb300 as dp
+    from dolphin_gb300._build import build_library
+    from dolphin_gb300.simulate import StackConfig, make_stack_torch
+
+    build_library()
+    frame = args.frame
+    stack = make_stack_torch(StackConfig(nslc=NSLC, rows=frame, cols=frame, seed=SEED, ps_frac=0.03))
+    plan = block_plan(frame, frame, BLOCK, HALF)
+    errs = {"tensor": [], "simt": []}
+    agg = {f: {"phase_max_rad": 0.0, "above_1e-3_rad": 0, "temp_coh_max": 0.0, "flips": 0, "flips_on_ps": 0,
+               "flips_fp64_emi": 0, "flips_phase_max_rad": 0.0, "coherent": 0} for f in errs}
+    secs = {"tensor": 0.0, "simt": 0.0, "fp64": 0.0}
+    glrt = {"tests": 0, "near_cutoff_1e-6": 0, "differ_from_float64": 0}
+    ps_near = ps_count = 0
+    for entry in plan:
+        blk, mean, disp, ps, nb = block_inputs(dp, stack, entry)
+        (t0, t1), (c0, c1) = entry[2], entry[3]
+        kw = dict(ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, compute_crlb=True)
+        outs = {}
+        for form in ("fp64", "tensor", "simt"):
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            outs[form] = dp.run_phase_linking(blk, HALF, covariance_form=form, **kw)
+            torch.cuda.synchronize()
+            secs[form] += time.perf_counter() - w0
+        trim = (slice(t0, t1), slice(c0, c1))
+        ref = outs["fp64"]
+        good = ref.temp_coh[trim] > 0.3
+        psm = ps.bool()[trim]
+        for form in errs:
+            o = outs[form]
+            d = torch.angle(o.cpx_phase[(slice(None),) + trim] * ref.cpx_phase[(slice(None),) + trim].conj())
+            d = d.abs().amax(0)
+            errs[form].append(d[good].float())
+            tcd = (o.temp_coh[trim] - ref.temp_coh[trim]).abs()[good]
+            flip = o.estimator[trim] != ref.estimator[trim]
+            a = agg[form]
+            a["coherent"] += int(good.sum())
+            a["phase_max_rad"] = max(a["phase_max_rad"], float(d[good].max()))
+            a["above_1e-3_rad"] += int((d[good] > 1e-3).sum())
+            a["temp_coh_max"] = max(a["temp_coh_max"], float(tcd.max()))
+            a["flips"] += int(flip.sum())
+            a["flips_on_ps"] += int((flip & psm).sum())
+            a["flips_fp64_emi"] += int((flip & (ref.estimator[trim] == 1)).sum())
+            if (flip & good).any():
+                a["flips_phase_max_rad"] = max(a["flips_phase_max_rad"], float(d[flip & good].max()))
+        tests, near, differ = glrt_check(torch, mean, disp, nb, NSLC, ALPHA)
+        glrt["tests"] += tests
+        glrt["near_cutoff_1e-6"] += near
+        glrt["differ_from_float64"] += differ
+        ps_near += int(((disp[trim] - PS_THR).abs() <= 1e-6 * PS_THR).sum())
+        ps_count += int(psm.sum())
+        del outs
+    for form in errs:
+        allv = torch.cat(errs[form])
+        agg[form]["phase_p99_rad"] = float(torch.quantile(allv[torch.randperm(allv.numel(), device=allv.device)[:2**24]],
+                                                          0.99))
+    print(json.dumps({
+        "workload": "parity",
+        "metric": f"phase error of the chosen form against the FP64 GPU form, N={NSLC} {frame}x{frame}",
+        "config": {"workload": f"N={NSLC} {frame}x{frame} stack (seed {SEED}), {BLOCK}x{BLOCK} blocks with halo, "
+                               f"half-window {HALF}, GLRT {ALPHA}, EMI, PS {PS_THR} + fill, CRLB; outputs trimmed "
+                               "to the blocks as the bench step keeps them", "blocks": len(plan)},
+        "chosen": agg["tensor"], "simt": agg["simt"],
+        "note": "per pixel the worst SLC's |angle(a conj b)|, on pixels whose FP64 temporal coherence is above 0.3; "
+                "flips = EMI/EVD choice differs from the FP64 form's",
+        "glrt": glrt, "ps": {"pixels": ps_count, "near_cutoff_1e-6": ps_near},
+        "seconds": {k: round(v, 2) for k, v in secs.items()},
+    }), flush=True)
+
+
+def run_peaks(args):
+    """FP32 and FP64 FMA rates (dpl_fp32_fma_probe, dpl_fp64_fma_probe: 8 CTAs of 256
+    threads per SM, 8 independent chains per thread, best of 5) and the TF32 tensor rate
+    (cuBLAS through torch.matmul with TF32 allowed, 8192^3, best of 10) of this GPU."""
+    import torch
+
+    from dolphin_gb300 import _lib
+    from dolphin_gb300._build import build_library
+
+    build_library()
+    lib = _lib.load()
+    dev = torch.cuda.current_device()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def probe(fn, dtype, iters):
+        blocks = sms * 8
+        out = torch.empty(blocks * 256, dtype=dtype, device="cuda")
+        _lib.check(fn(out.data_ptr(), blocks, iters, stream), "probe")
+        best = float("inf")
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.check(fn(out.data_ptr(), blocks, iters, stream), "probe")
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return blocks * 256 * 16.0 * iters / (best / 1000.0) / 1e12
+
+    torch.backends.cuda.matmul.allow_tf32 = True
+    a = torch.randn(8192, 8192, device="cuda")
+    b = torch.randn(8192, 8192, device="cuda")
+    for _ in range(3):
+        a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    print(json.dumps({"workload": "peaks", "unit": "TFLOP/s",
+                      "fp32_fma": probe(lib.dpl_fp32_fma_probe, torch.float32, 4096),
+                      "fp64_fma": probe(lib.dpl_fp64_fma_probe, torch.float64, 256),
+                      "tf32_cublas": 2 * 8192**3 / (best / 1000.0) / 1e12,
+                      "gpu": torch.cuda.get_device_name(dev)}), flush=True)
 
 
 BATCH_DEPTHS = (8, 10, 12, 15, 18, 20, 24, 28, 32, 36, 40, 45)
@@ -873,18 +1201,25 @@ def main():
     ap.add_argument("--frame", type=int, default=FRAME)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--workload", default="config2",
-                    choices=["config2", "precision", "batch", "similarity", "sequential", "learned"],
+                    choices=["config2", "precision", "batch", "similarity", "sequential", "learned", "parity",
+                             "peaks", "cpu-table"],
                     help="precision: N=40 2048x2048 stack, half-window (7, 7), low gamma_inf with a "
                          "high-coherence disk; rates of the tensor-core and SIMT covariance forms. "
                          "batch: 12 ministacks of N = 8..45, 1024x1024 each, as one CUDA graph. "
                          "similarity: median phase similarity, radius 7, of 30 interferograms. "
                          "sequential: the 30-SLC frame as ministacks of 15 with compressed SLCs. "
-                         "learned: EMI with and without the learned warm start, N=20")
+                         "learned: EMI with and without the learned warm start, N=20. "
+                         "parity: the chosen form against the FP64 GPU form over the whole N=30 frame. "
+                         "peaks: FP32, FP64 and TF32 rates of this GPU. "
+                         "cpu-table (with --impl reference): the CPU baseline table")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
-        run_reference(args, rank, world)
+        if args.workload == "cpu-table":
+            run_cpu_table(args)
+        else:
+            run_reference(args, rank, world)
         return
     if args.workload == "precision":
         run_precision(args)
@@ -900,6 +1235,12 @@ def main():
         return
     if args.workload == "learned":
         run_learned(args)
+        return
+    if args.workload == "parity":
+        run_parity(args)
+        return
+    if args.workload == "peaks":
+        run_peaks(args)
         return
     pool = None
     cores = len(os.sched_getaffinity(0))

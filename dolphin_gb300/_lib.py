@@ -92,6 +92,7 @@ SIGNATURES = {
     "dpl_process_coherence_noalloc": (_i, [_p, _i64, _i, _i, _d, _d, _i, _d, _i, _i, _p, _p, _p, _p, _p, _p, _p]),
     "dpl_kernel_timing": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "dpl_fp32_fma_probe": (_i, [_p, _i, _i, _p]),
+    "dpl_fp64_fma_probe": (_i, [_p, _i, _i, _p]),
 }
 
 _lock = threading.Lock()

@@ -50,3 +50,25 @@ extern "C" dpl_status dpl_fp32_fma_probe(float* out, int blocks, int iters, dpl_
     k_fma_peak<<<blocks, 256, 0, (cudaStream_t)stream>>>(out, iters);
     return dpl::check_launch("k_fma_peak");
 }
+
+// FP64 counterpart of k_fma_peak: 8 independent chains of double FMAs per thread.
+__global__ void __launch_bounds__(256) k_fma64_peak(double* out, int iters) {
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = threadIdx.x * 1e-3 + (double)k;
+#pragma unroll 8
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], 0.999999999, 1e-12);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+extern "C" dpl_status dpl_fp64_fma_probe(double* out, int blocks, int iters, dpl_stream_t stream) {
+    if (!out || blocks < 1 || iters < 1) return dpl::fail(DPL_ERR_INVALID_ARGUMENT, "dpl_fp64_fma_probe: bad argument");
+    k_fma64_peak<<<blocks, 256, 0, (cudaStream_t)stream>>>(out, iters);
+    return dpl::check_launch("k_fma64_peak");
+}

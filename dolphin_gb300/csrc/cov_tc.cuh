@@ -223,6 +223,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     // per-stage state as bit s: mbarrier phase parities, and (builders) an MMA commit on
     // empty[s] still to be consumed
     uint32_t ph_full = 0u, ph_empty = 0u, pend = 0u, ph_z = 0u;
+    // issuer: per sample buffer, bit c of z_arm = parity of the next phase it arms, bit c
+    // of z_used = armed at least once (to drain the copies in flight on a timeout)
+    uint32_t z_arm = 0u, z_used = 0u;
+    auto arm_bulk = [&](int c, int ch) {
+        const int zi = c & (kTcZBuf - 1);
+        tc_prefetch_bulk(a, zbuf(c), &zbar[zi], runs, ch);
+        z_arm ^= 1u << zi;
+        z_used |= 1u << zi;
+    };
     const int nchunks = a.kpad / kTcKC;
 
     const int ntiles = a.tiles_r * a.tiles_c;
@@ -390,7 +399,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 const uint64_t dA = tc_desc(tc_smem(sm + a.off_stage), LBO, SBO);
                 const uint64_t dB = dA + (uint64_t)((4 * 8192) >> 4);
                 if (bulk)
-                    for (int c = 0; c < kTcZBuf && c < nchunks; ++c) tc_prefetch_bulk(a, zbuf(c), &zbar[c], runs, c);
+                    for (int c = 0; c < kTcZBuf && c < nchunks; ++c) arm_bulk(c, c);
                 for (int ch = 0, s = 0; ch < nchunks; ++ch, s = s + 1 == a.nst ? 0 : s + 1) {
                     if (!tc_wait(&full[s], (ph_full >> s) & 1u)) {
                         atomicExch(sfail, 1);
@@ -424,8 +433,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                                      tc_smem(&empty[s]))
                                  : "memory");
                     // the builders are done with this chunk's samples: refill its buffer
-                    if (bulk && ch + kTcZBuf < nchunks)
-                        tc_prefetch_bulk(a, zbuf(ch), &zbar[ch & (kTcZBuf - 1)], runs, ch + kTcZBuf);
+                    if (bulk && ch + kTcZBuf < nchunks) arm_bulk(ch, ch + kTcZBuf);
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -483,6 +491,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
     if (tid == 0)
         for (int s2 = 0; s2 < a.nst; ++s2)
             if ((pend >> s2) & 1u) tc_wait(&empty[s2], (ph_empty >> s2) & 1u);
+    // and, after a timeout, that no bulk sample copy still writes into shared memory:
+    // the issuer waits (bounded) on the last phase it armed on each buffer, which has
+    // already completed where a builder consumed it
+    if (tid == kTcBuilders && *(volatile int*)sfail)
+        for (int c = 0; c < kTcZBuf; ++c)
+            if ((z_used >> c) & 1u) tc_wait(&zbar[c], ((z_arm >> c) & 1u) ^ 1u);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));

@@ -7,8 +7,12 @@
 // needs one more log, of the pooled scale.  Window starts follow lax.dynamic_slice
 // (clamped into the image: windows shift at the edges), validity follows the
 // unclamped origin and the window centre is always False -- the reference's
-// semantics.  Arithmetic order matches the reference's float32 expression
-// nslc * (2*log(pooled) - log(s1) - log(s2)) without FMA contraction.
+// semantics.  The statistic is the reference's float32 expression
+// nslc * (2*log(pooled) - log(s1) - log(s2)) without FMA contraction; its three logs
+// cancel, so its rounding is a few 1e-6 of the cutoff.  Where it lands within 1e-5
+// (relative) of the cutoff, the decision is taken on the same statistic evaluated in
+// double precision as nslc * log1p((s1 - s2)^2 / (4 s1 s2)) (algebraically equal, no
+// cancellation), so every mask bit is the exact comparison on the float32 scale^2.
 //
 // KS (shp/_ks.py:22-239): amplitudes are sorted per pixel (NaN last, like np.sort);
 // each (pixel, neighbour) pair walks the two-sample merge exactly as
@@ -81,6 +85,21 @@ __global__ void k_glrt_scale(const float* __restrict__ mean, const float* __rest
     int64_t r = i / cols, c = i - r * cols;
     float m = mean[i];
     scale2[r * pitch + c] = fdiv(fadd(var[i], fmul(m, m)), 2.f);
+}
+
+// One (pixel, offset) test: threshold > statistic, the float32 statistic refined in
+// double precision near the cutoff (see above).  NaN statistics stay False.
+__device__ __forceinline__ bool glrt_test(float s1, float s2, float l1, float l2, float nslc, float thr) {
+    // (s1 + s2) / 2 == (s1 + s2) * 0.5 exactly in IEEE arithmetic
+    const float pooled = fmul(fadd(s1, s2), 0.5f);
+    const float stat = fmul(nslc, fsub(fsub(fmul(2.f, logf(pooled)), l1), l2));
+    bool shp = thr > stat;
+    if (fabsf(stat - thr) <= 1e-5f * thr) {
+        const double d = (double)s1 - (double)s2;
+        const double t = (double)nslc * log1p(d * d / (4.0 * (double)s1 * (double)s2));
+        shp = (double)thr > t;
+    }
+    return shp;
 }
 
 template <bool kBits>
@@ -156,12 +175,8 @@ __global__ void __launch_bounds__(256) k_glrt(const __grid_constant__ CUtensorMa
                 const float* rlg = lg + (r0 + wa - rr0) * a.box_w + (c0 - x0);
                 for (int wb = 0; wb < wx; ++wb) {
                     bool shp = false;
-                    if (wb >= wb0 && wb < wb1 && !(wa == a.hy && wb == a.hx)) {
-                        // (s1 + s2) / 2 == (s1 + s2) * 0.5 exactly in IEEE arithmetic
-                        const float pooled = fmul(fadd(s1, rraw[wb]), 0.5f);
-                        const float stat = fmul(nslc, fsub(fsub(fmul(2.f, logf(pooled)), l1), rlg[wb]));
-                        shp = a.thr > stat;
-                    }
+                    if (wb >= wb0 && wb < wb1 && !(wa == a.hy && wb == a.hx))
+                        shp = glrt_test(s1, rraw[wb], l1, rlg[wb], nslc, a.thr);
                     dst[wb] = shp ? 1 : 0;
                 }
             }
@@ -191,9 +206,7 @@ __global__ void __launch_bounds__(256) k_glrt(const __grid_constant__ CUtensorMa
                 for (int wb = 0; wb < wx; ++wb) {
                     const bool valid = (wb >= -uc0) && (wb < a.cols - uc0) && !(wa == a.hy && wb == a.hx);
                     if (!valid) continue;
-                    const float pooled = fdiv(fadd(s1, rraw[wb]), 2.f);
-                    const float stat = fmul(nslc, fsub(fsub(fmul(2.f, logf(pooled)), l1), rlg[wb]));
-                    if (a.thr > stat) {
+                    if (glrt_test(s1, rraw[wb], l1, rlg[wb], nslc, a.thr)) {
                         if (wb < 32) w0 |= 1u << wb;
                         else w1 |= 1u << (wb - 32);
                     }

@@ -445,16 +445,15 @@ __global__ void __launch_bounds__(256, 3 - G) k_solve_reg(PixArgs a, RegLayout L
                 const float f = rme * rme;
                 Cf[me * ld + me] = cmake(f < 1e6f ? src[me] * f : 0.f, 0.f);
             }
-            for (int i = 1; i < n; ++i) {
-                const int o = i * (i - 1) / 2;
-                if (me < i) {
-                    const float f = rv[i] * rme;
-                    cfloat c = f < 1e6f ? cmake(src[n + 2 * (o + me)] * f, src[n + 2 * (o + me) + 1] * f)
-                                        : cmake(0.f, 0.f);
-                    if (lag > 0 && i - me >= lag) c = cmake(0.f, 0.f);
-                    Cf[i * ld + me] = c;
-                    Cf[me * ld + i] = cconj(c);
-                }
+            const int npairs = n * (n - 1) / 2;
+            for (int e = me; e < npairs; e += 32 * G) {
+                const uint32_t rc = ptab[e];
+                const int r = rc & 0xffff, c = rc >> 16;
+                const float f = rv[r] * rv[c];
+                cfloat v = f < 1e6f ? cmake(src[n + 2 * e] * f, src[n + 2 * e + 1] * f) : cmake(0.f, 0.f);
+                if (lag > 0 && r - c >= lag) v = cmake(0.f, 0.f);
+                Cf[r * ld + c] = v;
+                Cf[c * ld + r] = cconj(v);
             }
         } else {
             const cfloat* src = a.Cin + p * n * n;

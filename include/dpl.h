@@ -229,8 +229,8 @@ dpl_status dpl_compress(const float* slc, int64_t nslc, int64_t rows, int64_t co
 dpl_status dpl_circle_offsets(int max_radius, int min_radius, int sort_output, int32_t* offsets,
                               int64_t capacity, int64_t* count);
 
-/* Largest search_radius dpl_similarity accepts (11: every radius the reference's
- * workflows use, 7 and 11). */
+/* Largest search_radius dpl_similarity accepts (16; the reference's workflows use 7 and
+ * 11). */
 int dpl_similarity_max_radius(void);
 
 /* Replaces the preparation in _create_loop_and_run -- similarity.py:96-117 -- and, with
@@ -371,6 +371,13 @@ dpl_status dpl_kernel_timing(int enable, double* total_ms, int64_t* launches);
  * `blocks` x 256 threads, each running 8 independent chains of `iters` FMAs (16 * iters
  * flop per thread), and writes one float per thread to `out` (blocks * 256 floats). */
 dpl_status dpl_fp32_fma_probe(float* out, int blocks, int iters, dpl_stream_t stream);
+
+/* FP64 fused multiply-add throughput probe (no reference counterpart): the same shape
+ * as dpl_fp32_fma_probe in double precision -- `blocks` x 256 threads, 8 independent
+ * chains of `iters` double FMAs each (16 * iters flop per thread), one double per
+ * thread written to `out` (blocks * 256 doubles).  It measures the rate that decides
+ * which parts of the solver may run in FP64. */
+dpl_status dpl_fp64_fma_probe(double* out, int blocks, int iters, dpl_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -164,7 +164,7 @@ def _out_centers(out_n, stride):
 
 def estimate_neighbors_glrt(
     mean, var, halfwin_rowcol, strides=(1, 1), nslc=1, alpha=0.001, dtype=np.float32,
-    return_stat=False,
+    return_stat=False, exact=False,
 ):
     """shp/_glrt.py:13-130.
 
@@ -173,6 +173,11 @@ def estimate_neighbors_glrt(
     The comparison window is ``dynamic_slice``-clamped (shifted at edges), while the
     validity mask is taken from the unshifted window origin; the window centre
     ``[hy, hx]`` is always False.
+
+    ``exact``: decide on the statistic evaluated in float64 from the ``dtype`` scale^2,
+    as ``nslc * log1p((s1 - s2)^2 / (4 s1 s2))`` (algebraically the same, without the
+    cancellation of the three logs), against the ``dtype`` threshold.  The returned
+    statistic is then that float64 value.
     """
     dt = np.dtype(dtype)
     mean = np.asarray(mean, dtype=dt)
@@ -196,6 +201,10 @@ def estimate_neighbors_glrt(
     with np.errstate(all="ignore"):
         pooled = (s1 + s2) / 2
         stat = nslc * (2 * np.log(pooled) - np.log(s1) - np.log(s2))
+        if exact:
+            a1, a2 = s1.astype(np.float64), s2.astype(np.float64)
+            stat = float(nslc) * np.log1p((a1 - a2) ** 2 / (4.0 * a1 * a2))
+            thr = np.float64(thr)
     is_shp = thr > stat
     ur0 = in_r - hy
     uc0 = in_c - hx

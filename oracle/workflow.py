@@ -81,7 +81,9 @@ def _sl(a, b):
 
 
 def single(stack, hw, strides, block_shape, first_real, out_ref, comp_ref, nodata, ps, amp_mean, amp_disp,
-           shp_nslc, alpha, radius=7, method="glrt"):
+           shp_nslc, alpha, radius=7, method="glrt", dtype=np.float32):
+    """One ministack's block loop; ``dtype`` is the precision of the phase linking (the
+    SHP and PS selection stay float32, as the reference's)."""
     stack = np.asarray(stack)
     n, rows, cols = stack.shape
     sy, sx = strides
@@ -105,8 +107,8 @@ def single(stack, hw, strides, block_shape, first_real, out_ref, comp_ref, nodat
                                   amp_stack=np.abs(cur) if method == "ks" else None, method=method)
         try:
             res = P.run_phase_linking(cur, hw, strides, reference_idx=out_ref, nodata_mask=nodata[ir, ic],
-                                      ps_mask=ps[ir, ic], neighbor_arrays=nb, avg_mag=amp_mean[ir, ic],
-                                      first_real_slc_idx=first_real, compute_crlb=True)
+                                      ps_mask=ps[ir, ic].copy(), neighbor_arrays=nb, avg_mag=amp_mean[ir, ic],
+                                      first_real_slc_idx=first_real, compute_crlb=True, dtype=dtype)
         except P.PhaseLinkRuntimeError:
             continue
         tr, tc = _sl(t[0], t[1]), _sl(t[2], t[3])
@@ -131,14 +133,14 @@ def single(stack, hw, strides, block_shape, first_real, out_ref, comp_ref, nodat
 
 
 def sequential(stack, size, hw, strides, block_shape, nodata, ps, amp_mean, amp_disp, alpha=0.05, max_comp=100,
-               method="glrt"):
+               method="glrt", dtype=np.float32):
     """Per-ministack outputs, then the averages and the last ministack's radius-11 similarity."""
     stack = np.asarray(stack)
     comps, outs = [], []
     for layers, flags, oref, cref in plan(len(stack), size, max_comp):
         cur = np.stack([comps[-l - 1] if l < 0 else stack[l] for l in layers])
         res = single(cur, hw, strides, block_shape, flags.index(False), oref, cref, nodata, ps, amp_mean, amp_disp,
-                     len(stack), alpha, method=method)
+                     len(stack), alpha, method=method, dtype=dtype)
         comps.append(res["comp"])
         outs.append(res)
     extra = {}

@@ -233,7 +233,7 @@ def make_ps_fill():
         out[f"ka_r_{k}"], out[f"ka_c_{k}"] = np.asarray(r), np.asarray(c)
     out["n_ka"] = np.array(len(ka))
     # regression layout: PS positions of the reference's ps-fix fixture on a 522x534 grid
-    d = np.load("/root/reference/tests/data/ps-fix/failing_data_idxs.npz")
+    d = np.load(ref_shim.REF_ROOT / "tests" / "data" / "ps-fix" / "failing_data_idxs.npz")
     rows, cols = d["not_nan_rows"], d["not_nan_cols"]
     rng = np.random.default_rng(601)
     mags = (rng.normal(size=(522, 534)) ** 2).astype(np.float64)

@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import functools
 import importlib.util
+import os
 import sys
 import types
 from pathlib import Path
@@ -38,7 +39,9 @@ from pathlib import Path
 import numpy as np
 import scipy.linalg as sla
 
-REF_SRC = Path("/root/reference/src/dolphin")
+# the reference checkout: DOLPHIN_REF_ROOT, else where this container mounts it
+REF_ROOT = Path(os.environ.get("DOLPHIN_REF_ROOT", "/root/reference"))
+REF_SRC = REF_ROOT / "src" / "dolphin"
 
 # --------------------------------------------------------------------------------------
 # dtype canonicalisation (jax_enable_x64 = False)

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import phase_link as O
-from parity import phase_err
+from parity import judge_flips, phase_err
 
 pytestmark = pytest.mark.gpu
 
@@ -68,7 +68,9 @@ def test_full_block_crop_matches_oracle(block, r0, c0):
     crop = z[:, r0:r0 + 44, c0:c0 + 66].cpu().numpy()
     mean, disp, ps_c = O.calc_ps_block(np.abs(crop), PS_THR, N)
     nb_c = O.estimate_neighbors_glrt(mean, (disp * mean) ** 2, HALF, (1, 1), N, ALPHA)
-    ref = O.run_phase_linking(crop, HALF, ps_mask=ps_c, neighbor_arrays=nb_c, avg_mag=mean)
+    ref = O.run_phase_linking(crop, HALF, ps_mask=ps_c.copy(), neighbor_arrays=nb_c, avg_mag=mean)
+    ref64 = O.run_phase_linking(crop, HALF, ps_mask=ps_c.copy(), neighbor_arrays=nb_c, avg_mag=mean,
+                                dtype=np.float64)
     # interior of the crop, except where the crop touches the block's own edge
     ir0 = 0 if r0 == 0 else hy
     ic0 = 0 if c0 == 0 else hx
@@ -80,9 +82,14 @@ def test_full_block_crop_matches_oracle(block, r0, c0):
     np.testing.assert_array_equal(out.shp_counts.cpu().numpy()[sl], ref.shp_counts[rs])
     est_g, est_r = out.estimator.cpu().numpy()[sl], ref.estimator[rs]
     # EMI or EVD per pixel hangs on whether |Gamma| + 1e-6 I is positive definite, which
-    # rounding decides where |Gamma| is within rounding of singular (a few percent of these
-    # pixels); the comparisons below are on the pixels where both chose the same
-    assert np.mean(est_g != est_r) <= 0.05
+    # rounding decides where |Gamma| is within rounding of singular (PS pixels, whose few
+    # SHPs give a near rank-one |Gamma|): those pixels are judged against the float64 answer
+    mine = O.PhaseLinkOutput(*(np.asarray(x.cpu().numpy())[(slice(None),) * (x.dim() - 2) + sl]
+                               for x in out[:6]), None)
+    crop_ref = O.PhaseLinkOutput(*(np.asarray(x)[(slice(None),) * (x.ndim - 2) + rs] for x in ref[:6]), None)
+    crop_64 = O.PhaseLinkOutput(*(np.asarray(x)[(slice(None),) * (x.ndim - 2) + rs] for x in ref64[:6]), None)
+    flip = judge_flips(mine, crop_ref, crop_64, f"full-block crop ({r0}, {c0})")
+    assert not (flip & ~ps_c[rs]).any()
     tc_g, tc_r = out.temp_coh.cpu().numpy()[sl], ref.temp_coh[rs]
     good = (tc_r > 0.3) & (est_g == est_r)
     assert good.sum() > 0

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import phase_link as O
-from parity import compare_pl, phase_err
+from parity import compare_pl, judge_flips, phase_err
 
 pytestmark = pytest.mark.gpu
 
@@ -90,11 +90,48 @@ def test_glrt_vs_oracle(hw, strides):
     mean[:2, :3] = 0
     var[5, 7] = np.nan
     nb = dp.estimate_neighbors(halfwin_rowcol=hw, strides=strides, mean=mean, var=var, nslc=20, alpha=0.001)
-    ref, stat, thr = O.estimate_neighbors_glrt(mean, var, hw, strides, 20, 0.001, return_stat=True)
-    diff = nb != ref
-    # only pixels whose statistic is within float32 rounding of the cutoff may differ
-    near = np.abs(stat - thr) <= 1e-5 * thr
+    check_glrt_masks(nb, mean, var, hw, strides, 20, 0.001, f"GLRT {hw} {strides}")
+
+
+def check_glrt_masks(nb, mean, var, hw, strides, nslc, alpha, label):
+    """GLRT masks against the oracle: equal to the exact decision (the statistic in
+    float64 on the float32 scale^2) apart from tests within 1e-6 (relative) of the
+    cutoff, which are counted; against the float32 evaluation (the reference's
+    arithmetic) they differ only where float32 rounding flips that evaluation itself."""
+    ref, _stat, _thr = O.estimate_neighbors_glrt(mean, var, hw, strides, nslc, alpha, return_stat=True)
+    exact, xstat, xthr = O.estimate_neighbors_glrt(mean, var, hw, strides, nslc, alpha, return_stat=True,
+                                                   exact=True)
+    near = np.abs(xstat - xthr) <= 1e-6 * xthr
+    diff = nb != exact
     assert not (diff & ~near).any(), np.argwhere(diff & ~near)[:5]
+    flipped32 = ref != exact
+    diff32 = nb != ref
+    assert not (diff32 & ~(flipped32 | near)).any()
+    print(f"{label}: {int(near.sum())} tests within 1e-6 of the cutoff ({int((diff & near).sum())} of them "
+          f"differ from the exact decision); {int(flipped32.sum())} float32 decisions flipped by rounding")
+    return int(near.sum()), int((diff & near).sum()), int(flipped32.sum())
+
+
+def test_glrt_near_cutoff_is_exact():
+    """Neighbours whose statistic sits 1e-9 .. 1e-4 (relative) from the cutoff: every
+    GPU decision is the exact one, where the float32 evaluation flips some."""
+    from scipy import stats
+
+    nslc, alpha = 20, 0.001
+    thr = float(np.float32(stats.chi2.ppf(1 - alpha, df=1)))
+    c = np.expm1(thr / nslc)
+    r_star = ((2 + 4 * c) + np.sqrt((2 + 4 * c) ** 2 - 4)) / 2  # T(1, r*) = thr
+    deltas = np.concatenate([-np.logspace(-9, -4, 400), np.logspace(-9, -4, 400)])
+    s = np.ones(2 * deltas.size + 1, np.float64)
+    s[1::2] = r_star * (1 + deltas)
+    s = s.astype(np.float32)
+    # mean 0: scale^2 = var / 2 exactly
+    var = np.tile(2 * s, (3, 1)).astype(np.float32)
+    mean = np.zeros_like(var)
+    nb = dp.estimate_neighbors(halfwin_rowcol=(0, 1), mean=mean, var=var, nslc=nslc, alpha=alpha)
+    near, near_diff, flipped = check_glrt_masks(nb, mean, var, (0, 1), (1, 1), nslc, alpha, "GLRT near the cutoff")
+    assert near > 0 and near_diff == 0  # exact even within 1e-6 of the cutoff
+    assert flipped > 0  # where the float32 arithmetic flips decisions
 
 
 def test_glrt_window_larger_than_image():
@@ -272,12 +309,6 @@ def test_singular_gamma_falls_back_to_evd():
 # ---------------------------------------------------------------------------------
 # run_phase_linking end to end
 # ---------------------------------------------------------------------------------
-# |Gamma| + 1e-6 I closer to singular than this (float64 smallest eigenvalue) decides
-# EMI vs EVD by rounding: the tensor form perturbs C by ~1e-5, i.e. lambda_min by up
-# to ~N * 1e-5, so its band is wider.
-BORDER = {"simt": 1e-4, "tensor": 1e-3}
-
-
 @pytest.mark.parametrize("form", ["tensor", "simt"])
 def test_run_phase_linking_golden_cases(golden, form):
     g = golden("phase_link")
@@ -287,22 +318,20 @@ def test_run_phase_linking_golden_cases(golden, form):
         for key in ("ps_mask", "nodata_mask", "neighbor_arrays", "avg_mag"):
             if key in kw:
                 kw[key] = np.array(g[kw[key]])
-        diag = {}
         okw = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in kw.items()}
-        O.run_phase_linking(np.array(g[zname]), hw, strides, diagnostics=diag, **okw)
+        ref64 = O.run_phase_linking(np.array(g[zname]), hw, strides, dtype=np.float64, **okw)
         out = dp.run_phase_linking(np.array(g[zname]), hw, strides, covariance_form=form, **kw)
-        compare_pl(out, g, idx, borderline=diag["gamma_min_eig"] < BORDER[form])
+        compare_pl(out, g, idx, fp64=ref64, label=f"golden case {idx} ({form})")
 
 
 @pytest.mark.parametrize("form", ["tensor", "simt"])
 def test_config1_crop_golden(golden, form):
     g = golden("config1_crop")
-    diag = {}
-    O.run_phase_linking(g["slc"], (5, 5), (1, 1), ps_mask=g["ps"].copy(), neighbor_arrays=g["nb"],
-                        avg_mag=g["mean"], diagnostics=diag)
+    ref64 = O.run_phase_linking(g["slc"], (5, 5), (1, 1), ps_mask=g["ps"].copy(), neighbor_arrays=g["nb"],
+                                avg_mag=g["mean"], dtype=np.float64)
     out = dp.run_phase_linking(g["slc"], (5, 5), ps_mask=g["ps"], neighbor_arrays=g["nb"], avg_mag=g["mean"],
                                covariance_form=form)
-    compare_pl(out, g, "emi", borderline=diag["gamma_min_eig"] < BORDER[form])
+    compare_pl(out, g, "emi", fp64=ref64, label=f"config-1 crop ({form})")
 
 
 @pytest.mark.parametrize("strides", [1, 2, 3, 4, 5])
@@ -329,19 +358,21 @@ def test_config1_full_vs_oracle_f32_and_f64(form):
     var = (disp * mean) ** 2
     nb = dp.estimate_neighbors(halfwin_rowcol=(5, 5), alpha=0.001, mean=mean, var=var, nslc=10)
     out = dp.run_phase_linking(z, (5, 5), ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, covariance_form=form)
-    diag = {}
-    ref = O.run_phase_linking(z, (5, 5), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, diagnostics=diag)
+    ref = O.run_phase_linking(z, (5, 5), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean)
     ref64 = O.run_phase_linking(z, (5, 5), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, dtype=np.float64)
-    border = diag["gamma_min_eig"] < BORDER[form]
-    np.testing.assert_array_equal(out.estimator[~border], ref.estimator[~border])
-    good = (ref.temp_coh > 0.3) & ~border & np.all(np.isfinite(ref.cpx_phase), axis=0)
+    flip = judge_flips(out, ref, ref64, f"config 1 ({form})")
+    # against the FP64 oracle on every coherent pixel, flips included
+    good64 = (ref64.temp_coh > 0.3) & np.all(np.isfinite(ref64.cpx_phase), axis=0)
+    e64 = phase_err(out.cpx_phase[:, good64], ref64.cpx_phase[:, good64]).max()
+    assert e64 < PHASE_TOL, e64
+    assert np.abs(out.temp_coh[good64] - ref64.temp_coh[good64]).max() < TC_TOL
+    # against the float32 oracle where both chose the same estimator
+    good = (ref.temp_coh > 0.3) & ~flip & np.all(np.isfinite(ref.cpx_phase), axis=0)
     assert good.mean() > 0.5
     e32 = phase_err(out.cpx_phase[:, good], ref.cpx_phase[:, good]).max()
-    e64 = phase_err(out.cpx_phase[:, good], ref64.cpx_phase[:, good]).max()
     assert e32 < PHASE_TOL, e32
-    assert e64 < PHASE_TOL, e64
     assert np.abs(out.temp_coh[good] - ref.temp_coh[good]).max() < TC_TOL
-    assert np.abs(out.temp_coh[good] - ref64.temp_coh[good]).max() < TC_TOL
+    print(f"config 1 ({form}): max phase error {e32:.2e} rad vs float32, {e64:.2e} rad vs float64 oracle")
 
 
 def test_all_nan_slc_raises():
@@ -435,16 +466,19 @@ def test_config2_crop_tensor_vs_float64():
     mean, disp, ps = dp.calc_ps_block(np.abs(z), 0.25, 30)
     nb = dp.estimate_neighbors(halfwin_rowcol=(5, 11), alpha=0.001, mean=mean, var=(disp * mean) ** 2, nslc=30)
     out = dp.run_phase_linking(z, (5, 11), ps_mask=ps, neighbor_arrays=nb, avg_mag=mean)
-    diag = {}
-    ref64 = O.run_phase_linking(z, (5, 11), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean,
-                                dtype=np.float64, diagnostics=diag)
-    border = diag["gamma_min_eig"] < BORDER["tensor"]
-    good = (ref64.temp_coh > 0.3) & ~border & np.all(np.isfinite(ref64.cpx_phase), axis=0)
+    ref64 = O.run_phase_linking(z, (5, 11), ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, dtype=np.float64)
+    # every coherent pixel against the float64 oracle, estimator flips included
+    good = (ref64.temp_coh > 0.3) & np.all(np.isfinite(ref64.cpx_phase), axis=0)
     assert good.mean() > 0.8
     err = phase_err(out.cpx_phase[:, good], ref64.cpx_phase[:, good].astype(np.complex64))
     assert err.max() < PHASE_TOL, err.max()
     assert np.abs(out.temp_coh[good] - ref64.temp_coh[good]).max() < TC_TOL
-    np.testing.assert_array_equal(out.estimator[~border], ref64.estimator[~border])
+    flip = out.estimator != ref64.estimator
+    # the estimator differs only on PS pixels, whose phase PS filling replaces (their
+    # |Gamma| is near rank one, within float32 rounding of singular)
+    assert not (flip & ~ps.astype(bool)).any()
+    print(f"config-2 crop: max phase error {err.max():.2e} rad vs float64; {int(flip.sum())} estimator flips, "
+          f"all on PS pixels")
 
 
 # ---------------------------------------------------------------------------------
