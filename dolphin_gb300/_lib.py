@@ -37,6 +37,7 @@ class PlParams(C.Structure):
         ("use_evd", _i), ("beta", _d), ("zero_correlation_threshold", _d),
         ("reference_idx", _i), ("mask_input_ps", _i), ("use_max_ps", _i), ("use_slc_amp", _i),
         ("baseline_lag", _i), ("first_real_slc_idx", _i), ("compute_crlb", _i), ("cov_form", _i),
+        ("solver_slots", _i), ("solver_lanes", _i),
     ]
 
 

@@ -8,9 +8,11 @@ later ``run()`` calls replay it with one launch, reading the (updated in place)
 input tensors and writing the same output tensors.  The per-call status (all-NaN
 SLCs, device timeouts) is checked after the replay, as ``run_phase_linking`` does.
 
-The covariance form per N (tensor cores or SIMT) is chosen by ``tune_forms``, which
-times both on a small synthetic stack of that depth once per (N, half window,
-strides) and keeps the choice in a table that can be saved and loaded as JSON.
+Per N, ``tune_forms`` chooses the covariance form (tensor cores or SIMT) and the
+register solver's instance (row slots K and threads per pixel: several pixels per warp
+for small N) by timing the candidates on a small synthetic stack of that depth once per
+(N, half window, strides), and keeps the choice in a table that can be saved and loaded
+as JSON.
 """
 
 from __future__ import annotations
@@ -28,18 +30,60 @@ from .shp import estimate_neighbors
 
 __all__ = ["PhaseLinkBatch", "tune_forms"]
 
-_TUNED: dict[tuple, str] = {}
+_TUNED: dict[tuple, dict] = {}
 
 
-def tune_forms(depths, half_window, strides=(1, 1), table_path=None, sample=96, reps=3):
-    """Pick the faster covariance form for each stack depth; returns {N: form}.
+def _solver_candidates(n):
+    """(slots, lanes) pairs the register solver offers for depth n: K = n rounded up to
+    even and the next power of two (one or two warps as n needs), and every group size
+    from the smallest that fits K up to a whole warp."""
+    k0 = max(4, (n + 1) & ~1)
+    ks = {k0}
+    p2 = 4
+    while p2 < k0:
+        p2 *= 2
+    if p2 <= 64 and (p2 > 32) == (k0 > 32):
+        ks.add(p2)
+    out = []
+    for k in sorted(ks):
+        if k > 32:
+            out.append((k, 64))
+            continue
+        g = 8
+        while g < k:
+            g *= 2
+        while g <= 32:
+            out.append((k, g))
+            g *= 2
+    return out
 
-    Timings use a seeded synthetic stack of ``sample x sample`` output pixels per depth.
-    ``table_path`` (JSON) is read first and written back with any new entries.
-    """
+
+def _time_call(fn, reps):
     import torch
 
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def tune_forms(depths, half_window, strides=(1, 1), table_path=None, sample=192, reps=3):
+    """Pick, for each stack depth N, the covariance form (tensor cores or SIMT) and the
+    register solver's instance (row slots K and threads per pixel) by timing the
+    candidates; returns {N: {"form": ..., "slots": K, "lanes": G}}.
+
+    Timings use a seeded synthetic stack of ``sample x sample`` output pixels per depth,
+    with its GLRT SHPs.  ``table_path`` (JSON) is read first and written back with any
+    new entries.
+    """
     from .phase_link import run_phase_linking
+    from .ps import calc_ps_block as _ps
+    from .shp import estimate_neighbors as _shp
     from .simulate import StackConfig, make_stack_torch
 
     hy, hx = (int(v) for v in half_window)
@@ -50,37 +94,46 @@ def tune_forms(depths, half_window, strides=(1, 1), table_path=None, sample=96, 
     out = {}
     for n in sorted(set(int(d) for d in depths)):
         key = (n, hy, hx, sy, sx)
-        if key not in _TUNED:
+        if key not in _TUNED or not isinstance(_TUNED[key], dict):
             cfg = StackConfig(nslc=n, rows=sample * sy + 2 * hy, cols=sample * sx + 2 * hx, seed=1000 + n,
-                              ps_frac=0.0)
+                              ps_frac=0.03)
             z = make_stack_torch(cfg)
-            best, best_ms = None, float("inf")
-            for form in ("tensor", "simt"):
-                run_phase_linking(z, (hy, hx), (sy, sx), compute_crlb=False, covariance_form=form)
-                torch.cuda.synchronize()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                for _ in range(reps):
-                    run_phase_linking(z, (hy, hx), (sy, sx), compute_crlb=False, covariance_form=form)
-                e1.record()
-                torch.cuda.synchronize()
-                ms = e0.elapsed_time(e1) / reps
-                if ms < best_ms:
-                    best, best_ms = form, ms
-            _TUNED[key] = best
-        out[n] = _TUNED[key]
+            mean, disp, ps = _ps(z.abs(), 0.25, n)
+            nb = _shp(halfwin_rowcol=(hy, hx), alpha=0.001, strides=(sy, sx), mean=mean, var=(disp * mean) ** 2,
+                      nslc=n)
+            kw = dict(ps_mask=ps, neighbor_arrays=nb, avg_mag=mean)
+            forms = {f: _time_call(lambda f=f: run_phase_linking(z, (hy, hx), (sy, sx), covariance_form=f, **kw), reps)
+                     for f in ("tensor", "simt")}
+            form = min(forms, key=forms.get)
+            solver = {}
+            for k, g in _solver_candidates(n):
+                solver[(k, g)] = _time_call(lambda k=k, g=g: run_phase_linking(
+                    z, (hy, hx), (sy, sx), covariance_form=form, solver_slots=k, solver_lanes=g, **kw), reps)
+            k, g = min(solver, key=solver.get)
+            _TUNED[key] = {"form": form, "slots": k, "lanes": g,
+                           "ms": {"forms": {f: round(v, 4) for f, v in forms.items()},
+                                  "solver": {f"{kk},{gg}": round(v, 4) for (kk, gg), v in solver.items()}}}
+        out[n] = {k: v for k, v in _TUNED[key].items() if k != "ms"}
     if table_path is not None:
         Path(table_path).write_text(json.dumps({",".join(map(str, k)): v for k, v in sorted(_TUNED.items())},
                                                indent=1))
     return out
 
 
+def _choice(forms, n):
+    """A tuned entry as (form, slots, lanes); a bare form string means default slots."""
+    c = forms.get(n, "tensor")
+    if isinstance(c, str):
+        return c, 0, 0
+    return c.get("form", "tensor"), int(c.get("slots", 0)), int(c.get("lanes", 0))
+
+
 class PhaseLinkBatch:
     """PS + GLRT + phase linking over a list of (N_k, rows, cols) complex64 CUDA stacks.
 
     Parameters follow ``run_phase_linking`` (EMI/EVD, CRLB, references) and
-    ``estimate_neighbors`` (GLRT ``alpha``); ``forms`` maps N to "tensor" or "simt"
-    (default: ``tune_forms``).  ``graph=False`` runs every call eagerly.
+    ``estimate_neighbors`` (GLRT ``alpha``); ``forms`` maps N to a ``tune_forms`` entry
+    or to a bare covariance form, "tensor" or "simt" (default: ``tune_forms``).  ``graph=False`` runs every call eagerly.
     """
 
     def __init__(self, stacks, half_window, strides=(1, 1), alpha=0.001, ps_threshold=0.25, use_evd=False,
@@ -113,11 +166,12 @@ class PhaseLinkBatch:
             nb = estimate_neighbors(halfwin_rowcol=self.hw, alpha=self.alpha, strides=self.st, mean=mean,
                                     var=(disp * mean) ** 2, nslc=n)
             orow, ocol = rows // sy, cols // sx
+            form, slots, lanes = _choice(self.forms, n)
             prm = _lib.PlParams(nslc=n, rows=rows, cols=cols, hy=hy, hx=hx, sy=sy, sx=sx,
                                 use_evd=int(self.use_evd), beta=0.0, zero_correlation_threshold=0.0,
                                 reference_idx=self.ref, mask_input_ps=0, use_max_ps=1, use_slc_amp=0,
                                 baseline_lag=0, first_real_slc_idx=0, compute_crlb=int(self.crlb),
-                                cov_form=_form_code(self.forms.get(n, "tensor")))
+                                cov_form=_form_code(form), solver_slots=slots, solver_lanes=lanes)
             o = {
                 "cpx": torch.empty((n, orow, ocol), dtype=torch.complex64, device=z.device),
                 "tc": torch.empty((orow, ocol), dtype=torch.float32, device=z.device),

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "dpl_common.cuh"
+#include "pix_args.cuh"
 
 namespace dpl {
 
@@ -107,81 +108,9 @@ __global__ void __launch_bounds__(256) k_prep(const cfloat* __restrict__ slc, in
     }
 }
 
-// ---------------------------------------------------------------------------------
-// k_pixel: per-warp shared-memory layout
-// ---------------------------------------------------------------------------------
-// C (packed complex) | W1 (packed real) | S: staging for the window rows, or R (packed
-// complex) + W2 (packed real), or the full n x n LU of the fallback | v | d | piv
-struct PixLayout {
-    int n, np, stg, ldg;
-    size_t off_C, off_G, off_S, off_v, off_d, off_piv, bytes;
-};
-
-// C (packed complex) | G (n x ldg real) | S: staging for the covariance's window rows,
-// or R (packed complex), or the full n x n LU of the LU pass | v | d | piv
-inline PixLayout make_layout(int n, int wx, bool lu) {
-    PixLayout L{};
-    const size_t T = (size_t)n * (n + 1) / 2;
-    L.n = n;
-    L.np = (n + 1) & ~1;
-    L.stg = wx * L.np + 32;
-    L.ldg = n | 1;
-    size_t o = 0;
-    auto take = [&](size_t bytes) {
-        size_t at = o;
-        o = align_up(o + bytes, 16);
-        return at;
-    };
-    L.off_C = take(T * sizeof(cfloat));
-    L.off_G = take((size_t)n * L.ldg * sizeof(float));
-    size_t s_bytes = std::max((size_t)L.stg * sizeof(cfloat), T * sizeof(cfloat));
-    if (lu) s_bytes = std::max(s_bytes, (size_t)n * n * sizeof(cfloat));
-    L.off_S = take(s_bytes);
-    L.off_v = take(64 * sizeof(cfloat));
-    L.off_d = take(64 * sizeof(float));
-    L.off_piv = take(128 * sizeof(int));
-    L.bytes = align_up(o, 128);
-    return L;
-}
-
-enum PixMode { kCovOnly = 0, kSolveOnly = 1, kFused = 2 };
-
-struct PixArgs {
-    int n, rows, cols, hy, hx, sy, sx, out_rows, out_cols;
-    int64_t npix;
-    int np, stg, ldg;
-    size_t off_C, off_G, off_S, off_v, off_d, off_piv, warp_bytes;
-    const cfloat* zt;        // (rows, cols, n) masked, pixel-major
-    const uint8_t* nb_u8;    // (out_rows, out_cols, wy, wx) or null
-    const uint32_t* nb_bits; // (out_rows, out_cols, wy, wpr) or null
-    int wpr;
-    const cfloat* Cin;       // solve-only input: (npix, n, n)
-    const cfloat* vstart;    // optional EMI starting vectors (npix, n); plain start when null
-    int16_t* iters;          // optional: eigen-iterations used per pixel (npix)
-    const float* Cplanar;    // solve-only input, planar per pixel: diagonal | (Re, Im) per lower pair
-    int use_evd, beta_on;
-    float one_minus_beta, beta, zct;
-    int ref_idx, compute_crlb, crlb_ref, baseline_lag;
-    float crlb_factor;
-    double beta_d, zct_d, crlb_factor_d;  // the same parameters unrounded (FP64 form)
-    cfloat* Cout;            // cov-only output: (npix, n, n)
-    cfloat* vout;            // (npix, n) referenced eigenvectors
-    float* eig;
-    uint8_t* est;
-    float* crlb;             // (npix, n)
-    float* tcoh;
-    float* closure;          // (npix, n - 2) or null
-    int32_t* counts;         // (npix) or null
-    int* fb_list;            // pixels whose EMI shifted matrix is indefinite (for the LU pass)
-    int* fb_count;
-    const int* list;         // LU pass: pixels list[0 .. *list_count)
-    const int* list_count;
-};
-
 }  // namespace dpl
 
 #include "solver.cuh"
-#include "solver_reg.cuh"
 
 namespace dpl {
 
@@ -511,29 +440,25 @@ static dpl_status launch_pixel_pass(const PixArgs& a, cudaStream_t s) {
     return go(k_pixel<2, MODE, kLU>);
 }
 
-// Register-resident solve pass for n <= 64: 8 warps per CTA, one pixel per warp
-// (n <= 32) or per pair of warps (n <= 64).
-static dpl_status launch_solve_reg(const PixArgs& a, cudaStream_t s) {
-    const RegLayout L = make_reg_layout(a.n);
-    const int warps = 8;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    auto go = [&](auto kernel, int group_warps) -> dpl_status {
-        const int groups = warps / group_warps;
-        const size_t smem = (size_t)groups * L.bytes + (size_t)a.n * (a.n - 1) / 2 * sizeof(uint32_t);
-        if (smem > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "register solver: shared memory exceeds the SM limit");
-        DPL_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int per_sm = 0;
-        DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, warps * 32, smem));
-        const int64_t resident = (int64_t)std::max(1, per_sm) * std::max(1, sms);
-        const int64_t grid = std::min<int64_t>((a.npix + groups - 1) / groups, resident * 8);
-        kernel<<<(unsigned)std::max<int64_t>(grid, 1), warps * 32, smem, s>>>(a, L);
-        return check_launch("k_solve_reg");
-    };
-    if (a.n <= 16) return go(k_solve_reg<16, 1>, 1);
-    if (a.n <= 32) return go(k_solve_reg<32, 1>, 1);
-    return go(k_solve_reg<64, 2>, 2);
+// ---------------------------------------------------------------------------------
+// register-solver dispatch: K = n rounded up to even (at least 4), or a.slots when
+// that is larger (a tuned choice); G threads per pixel from solver_lanes
+// ---------------------------------------------------------------------------------
+dpl_status launch_solve_reg_a(int K, int G, const PixArgs& a, cudaStream_t s);
+dpl_status launch_solve_reg_b(int K, int G, const PixArgs& a, cudaStream_t s);
+dpl_status launch_solve_reg_c(int K, int G, const PixArgs& a, cudaStream_t s);
+dpl_status launch_solve_reg_d(int K, int G, const PixArgs& a, cudaStream_t s);
+dpl_status launch_solve_reg_e(int K, int G, const PixArgs& a, cudaStream_t s);
+
+dpl_status launch_solve_reg(const PixArgs& a, cudaStream_t s) {
+    int K = std::max(4, (a.n + 1) & ~1);
+    if (a.slots > K && a.slots <= 64 && (a.slots & 1) == 0 && (K > 32) == (a.slots > 32)) K = a.slots;
+    const int G = solver_lanes(K, a.lanes);
+    if (K <= 16) return launch_solve_reg_a(K, G, a, s);
+    if (K <= 32) return launch_solve_reg_b(K, G, a, s);
+    if (K <= 44) return launch_solve_reg_c(K, G, a, s);
+    if (K <= 54) return launch_solve_reg_d(K, G, a, s);
+    return launch_solve_reg_e(K, G, a, s);
 }
 
 // Main pass (Cholesky inverse iteration) and, for the pixels it lists, the LU pass.
@@ -768,6 +693,8 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
         set_solver_params(a, P.use_evd, P.beta, P.zero_correlation_threshold, ref, std::sqrt((double)P.hy * P.hx),
                           P.first_real_slc_idx, P.compute_crlb);
         a.baseline_lag = P.baseline_lag > 0 ? P.baseline_lag : 0;
+        a.slots = P.solver_slots;
+        a.lanes = P.solver_lanes;
         a.vout = w.V;
         a.eig = out->eigenvalues;
         a.est = out->estimator;

@@ -101,7 +101,7 @@ __device__ bool s_gauss_jordan_spd(float* A, int n, int ld, int lane) {
 }
 
 // Complex Cholesky in place on packed R (Hermitian, lower stored); dinv[k] = 1/R_kk.
-__device__ bool s_chol_complex(cfloat* R, float* dinv, int n, int lane) {
+__device__ inline bool s_chol_complex(cfloat* R, float* dinv, int n, int lane) {
     for (int k = 0; k < n; ++k) {
         __syncwarp();
         const float d = R[pk(k, k)].re;
@@ -184,7 +184,7 @@ __device__ void s_chol_solve(const cfloat* R, const float* dinv, int n, cfloat (
 
 // LU with partial pivoting (getrf: first maximum of |re| + |im|) on a full n x n
 // matrix (ld = n); piv[k] = pivot row of step k.
-__device__ void s_lu(cfloat* A, int n, int* piv, int lane) {
+__device__ inline void s_lu(cfloat* A, int n, int* piv, int lane) {
     for (int k = 0; k < n; ++k) {
         __syncwarp();
         float best = -1.f;

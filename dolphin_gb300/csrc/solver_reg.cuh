@@ -50,23 +50,34 @@ inline RegLayout make_reg_layout(int n) {
     return L;
 }
 
-// A pixel group of G warps (G = 1 or 2): row index, synchronisation and reductions.
+// A pixel group of G threads: G = 8, 16 or 32 lanes of one warp (a warp holds 32 / G
+// pixels) or G = 64, two whole warps: row index, synchronisation, reductions.
 template <int G>
 struct Grp {
-    int gl;      // thread (= row) index within the group, 0 .. 32G - 1
-    int lane;    // lane within its warp
-    int wig;     // warp within the group
-    int bar;     // named barrier of the group (G == 2)
-    float* x;    // reduction slots (shared memory, 16 floats)
+    int gl;         // thread (= row) index within the group, 0 .. G - 1
+    int lane;       // lane within its warp
+    int wig;        // warp within the group (G == 64)
+    int bar;        // named barrier of the group (G == 64)
+    int base;       // first lane of the group in its warp (G <= 32)
+    unsigned mask;  // the group's lanes (G <= 32)
+    float* x;       // reduction slots (shared memory, 16 floats)
 
     __device__ __forceinline__ void sync() const {
-        __syncwarp();  // bar.sync counts a warp as arrived when any of its lanes arrives
-        if (G > 1) asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(32 * G) : "memory");
+        if (G <= 32) {
+            __syncwarp(mask);
+        } else {
+            __syncwarp();  // bar.sync counts a warp as arrived when any of its lanes arrives
+            asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(64) : "memory");
+        }
     }
     // sum over the group, the same value in every thread
     __device__ __forceinline__ float sum(float v) const {
+        if (G <= 32) {
+#pragma unroll
+            for (int o = (G >> 1); o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+            return v;
+        }
         v = warp_sum(v);
-        if (G == 1) return v;
         if (lane == 0) x[wig] = v;
         sync();
         const float r = x[0] + x[1];
@@ -74,8 +85,8 @@ struct Grp {
         return r;
     }
     __device__ __forceinline__ bool any(bool v) const {
+        if (G <= 32) return __any_sync(mask, v);
         v = warp_any(v);
-        if (G == 1) return v;
         if (lane == 0) x[2 + wig] = v ? 1.f : 0.f;
         sync();
         const bool r = x[2] + x[3] > 0.f;
@@ -84,7 +95,7 @@ struct Grp {
     }
     // value of thread k (uniform k)
     __device__ __forceinline__ cfloat bcast(cfloat v, int k) const {
-        if (G == 1) return shfl_c(v, k);
+        if (G <= 32) return {__shfl_sync(mask, v.re, base + k), __shfl_sync(mask, v.im, base + k)};
         if (gl == k) {
             x[4] = v.re;
             x[5] = v.im;
@@ -96,6 +107,15 @@ struct Grp {
     }
 };
 
+// Broadcast position of row `row`'s pivot-column entry before step k: (row - k) mod K
+// (slot s of every row then reads position s).  K is even; row, k < K.
+template <int K>
+__device__ __forceinline__ int slot_pos(int row, int k) {
+    if ((K & (K - 1)) == 0) return (row - k) & (K - 1);
+    const int d = row - k;
+    return d < 0 ? d + K : d;
+}
+
 // Real symmetric sweep over indices 0..n-1 of the matrix whose row `gl` is g; on
 // success g holds row `gl` of -A^{-1}.  Returns false (uniformly) if any pivot was
 // <= 0 (the remaining steps then run on meaningless values, without branching).
@@ -105,7 +125,7 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, const 
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
         gr.sync();
-        if (gr.gl < K) buf[(gr.gl - k) & (K - 1)] = g[0];  // A[row][k] (= A[k][row])
+        if (gr.gl < K) buf[slot_pos<K>(gr.gl, k)] = g[0];  // A[row][k] (= A[k][row])
         gr.sync();
         float r[K];
         const float4* b4 = reinterpret_cast<const float4*>(buf);
@@ -116,6 +136,11 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, const 
             r[4 * q + 1] = t.y;
             r[4 * q + 2] = t.z;
             r[4 * q + 3] = t.w;
+        }
+        if (K % 4) {  // K = 4m + 2: the last two slots
+            const float2 t = reinterpret_cast<const float2*>(buf)[K / 2 - 1];
+            r[K - 2] = t.x;
+            r[K - 1] = t.y;
         }
         const float p = r[0];
         bad |= !(p > 0.f);
@@ -147,7 +172,7 @@ __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, co
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
         gr.sync();
-        if (gr.gl < K) buf[(gr.gl - k) & (K - 1)] = a[0];  // A[row][k] = conj(A[k][row])
+        if (gr.gl < K) buf[slot_pos<K>(gr.gl, k)] = a[0];  // A[row][k] = conj(A[k][row])
         gr.sync();
         const float p = buf[0].re;
         bad |= !(p > 0.f);
@@ -197,7 +222,7 @@ __device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloa
 template <int G>
 __device__ __forceinline__ void r_prefetch(float* dst, const float* src, int count, const Grp<G>& gr) {
     gr.sync();
-    for (int e = gr.gl; e < count; e += 32 * G)
+    for (int e = gr.gl; e < count; e += G)
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + e)),
                      "l"(src + e)
                      : "memory");
@@ -377,7 +402,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     gr.sync();
     float sre = 0.f, sim = 0.f, cnt = 0.f;
     const int npairs = n * (n - 1) / 2;
-    for (int e = me; e < npairs; e += 32 * G) {
+    for (int e = me; e < npairs; e += G) {
         const uint32_t rc = ptab[e];
         const int r = rc & 0xffff, c = rc >> 16;
         const cfloat u = fphasor(Cf[r * ld + c]);
@@ -403,15 +428,30 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
 // lower pair (i, j), i > j, at o = i(i-1)/2 + j) or as full (npix, n, n) matrices
 // of which the lower triangle is read.
 template <int K, int G>
-__global__ void __launch_bounds__(256, 3 - G) k_solve_reg(PixArgs a, RegLayout L) {
+__global__ void __launch_bounds__(256, G == 64 ? 1 : 2) k_solve_reg(PixArgs a, RegLayout L) {
     extern __shared__ __align__(16) unsigned char reg_smem[];
-    const int warp = threadIdx.x >> 5, ngroups = (blockDim.x >> 5) / G;
-    const int group = warp / G;
+    const int warp = threadIdx.x >> 5;
     Grp<G> gr;
     gr.lane = threadIdx.x & 31;
-    gr.wig = warp - group * G;
-    gr.gl = gr.wig * 32 + gr.lane;
-    gr.bar = 1 + group;
+    int group, ngroups;
+    if (G <= 32) {
+        constexpr int per_warp = 32 / (G <= 32 ? G : 32);
+        ngroups = (blockDim.x >> 5) * per_warp;
+        group = warp * per_warp + gr.lane / G;
+        gr.base = gr.lane & ~(G - 1);
+        gr.mask = G == 32 ? 0xffffffffu : ((1u << (G & 31)) - 1u) << gr.base;
+        gr.wig = 0;
+        gr.gl = gr.lane - gr.base;
+        gr.bar = 0;
+    } else {
+        ngroups = (blockDim.x >> 5) / 2;
+        group = warp / 2;
+        gr.base = 0;
+        gr.mask = 0xffffffffu;
+        gr.wig = warp - group * 2;
+        gr.gl = gr.wig * 32 + gr.lane;
+        gr.bar = 1 + group;
+    }
     unsigned char* base = reg_smem + group * L.bytes;
     gr.x = reinterpret_cast<float*>(base + L.off_x);
     cfloat* Cf = reinterpret_cast<cfloat*>(base + L.off_C);
@@ -446,7 +486,7 @@ __global__ void __launch_bounds__(256, 3 - G) k_solve_reg(PixArgs a, RegLayout L
                 Cf[me * ld + me] = cmake(f < 1e6f ? src[me] * f : 0.f, 0.f);
             }
             const int npairs = n * (n - 1) / 2;
-            for (int e = me; e < npairs; e += 32 * G) {
+            for (int e = me; e < npairs; e += G) {
                 const uint32_t rc = ptab[e];
                 const int r = rc & 0xffff, c = rc >> 16;
                 const float f = rv[r] * rv[c];
@@ -472,6 +512,27 @@ __global__ void __launch_bounds__(256, 3 - G) k_solve_reg(PixArgs a, RegLayout L
         staged = next != nullptr;
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// Host launch of the instance with K slots and G threads per pixel: 8 warps per CTA,
+// 256 / G pixel groups; a persistent grid of at most 8 waves.
+template <int K, int G>
+dpl_status launch_solve_reg_k(const PixArgs& a, cudaStream_t s) {
+    const RegLayout L = make_reg_layout(a.n);
+    const int warps = 8;
+    const int groups = warps * 32 / G;
+    const size_t smem = (size_t)groups * L.bytes + (size_t)a.n * (a.n - 1) / 2 * sizeof(uint32_t);
+    if (smem > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "register solver: shared memory exceeds the SM limit");
+    int dev = 0, sms = 0;
+    DPL_CUDA_TRY(cudaGetDevice(&dev));
+    DPL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DPL_CUDA_TRY(cudaFuncSetAttribute(k_solve_reg<K, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_reg<K, G>, warps * 32, smem));
+    const int64_t resident = (int64_t)std::max(1, per_sm) * std::max(1, sms);
+    const int64_t grid = std::min<int64_t>((a.npix + groups - 1) / groups, resident * 8);
+    k_solve_reg<K, G><<<(unsigned)std::max<int64_t>(grid, 1), warps * 32, smem, s>>>(a, L);
+    return check_launch("k_solve_reg");
 }
 
 }  // namespace dpl

@@ -118,6 +118,8 @@ def run_phase_linking(
     compute_crlb: bool = True,
     *,
     covariance_form: str = "tensor",
+    solver_slots: int = 0,
+    solver_lanes: int = 0,
 ) -> PhaseLinkOutput:
     """Estimate the linked phase for a stack of SLCs (phase_link/_core.py:67-249).
 
@@ -129,6 +131,11 @@ def run_phase_linking(
     accumulation); ``"simt"`` uses fp32 CUDA-core arithmetic throughout; ``"fp64"``
     computes the covariance and the solve in double precision (a reference form: GB300's
     FP64 rate is low), writing the same float32 outputs.
+
+    ``solver_slots`` / ``solver_lanes`` (keyword-only, not in the reference): the
+    register solver's row slots (even, >= N) and threads per pixel (8, 16, 32); 0 picks
+    the smallest that fit.  A tuner's choices (``dolphin_gb300.tune_forms``); the results
+    are the same.
     """
     on_device = D.is_device_tensor(slc_stack)
     shape = tuple(slc_stack.shape)
@@ -168,7 +175,7 @@ def run_phase_linking(
         use_max_ps=int(bool(use_max_ps)), use_slc_amp=int(bool(use_slc_amp)),
         baseline_lag=int(baseline_lag) if baseline_lag else 0,
         first_real_slc_idx=int(first_real_slc_idx), compute_crlb=int(bool(compute_crlb)),
-        cov_form=_form_code(covariance_form),
+        cov_form=_form_code(covariance_form), solver_slots=int(solver_slots), solver_lanes=int(solver_lanes),
     )
     cpx = D.empty((nslc, out_rows, out_cols), np.complex64)
     tcoh = D.empty((out_rows, out_cols), np.float32)

@@ -122,6 +122,12 @@ typedef struct dpl_pl_params {
     int compute_crlb;
     int cov_form;                  /* 0: tensor-core covariance (default); 1: SIMT covariance (plain form);
                                       2: covariance and solver in FP64 (the double-precision reference form) */
+    /* Not in the reference (zero = default).  Register-solver instance: row slots K (even,
+     * >= nslc; 0 = nslc rounded up to even) and threads per pixel (8, 16 or 32 for K <= 32;
+     * 0 = the smallest power of two >= K); a tuner's choices: the same algorithm, group
+     * reductions may round differently. */
+    int solver_slots;
+    int solver_lanes;
 } dpl_pl_params;
 
 typedef struct dpl_pl_inputs {

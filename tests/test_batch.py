@@ -73,5 +73,30 @@ def test_batch_reports_all_nan_slc_after_replay():
 def test_tune_forms_table(tmp_path):
     path = tmp_path / "forms.json"
     forms = tune_forms([8, 20], HW, table_path=path, sample=32, reps=1)
-    assert set(forms) == {8, 20} and set(forms.values()) <= {"tensor", "simt"}
+    assert set(forms) == {8, 20}
+    for n, c in forms.items():
+        assert c["form"] in {"tensor", "simt"}
+        assert c["slots"] >= n and c["slots"] % 2 == 0 and c["lanes"] in (8, 16, 32) and c["lanes"] >= c["slots"]
     assert path.exists() and tune_forms([8], HW, table_path=path) == {8: forms[8]}
+
+
+@pytest.mark.parametrize("n", [6, 8, 12, 20, 30, 45])
+def test_solver_instances_agree(n):
+    """Every register-solver instance the tuner can pick (row slots, threads per pixel)
+    gives the default instance's results, up to the order of the group reductions."""
+    from dolphin_gb300.batch import _solver_candidates
+
+    z = _stacks(990 + n, depths=(n,))[0]
+    mean, disp, ps = dp.calc_ps_block(z.abs(), 0.25, n)
+    nb = dp.estimate_neighbors(halfwin_rowcol=HW, alpha=0.001, mean=mean, var=(disp * mean) ** 2, nslc=n)
+    kw = dict(ps_mask=ps, neighbor_arrays=nb, avg_mag=mean)
+    ref = dp.run_phase_linking(z, HW, **kw)
+    for k, g in _solver_candidates(n):
+        out = dp.run_phase_linking(z, HW, solver_slots=k, solver_lanes=g, **kw)
+        assert torch.equal(out.estimator, ref.estimator), (k, g)
+        good = torch.isfinite(ref.cpx_phase).all(0) & (ref.temp_coh > 0.3)
+        err = torch.angle(out.cpx_phase[:, good] * ref.cpx_phase[:, good].conj()).abs().max()
+        assert float(err) < 1e-5, (k, g, float(err))
+        assert float((out.temp_coh - ref.temp_coh)[good].abs().max()) < 1e-5
+        fin = torch.isfinite(ref.crlb_std_dev)
+        assert torch.equal(fin, torch.isfinite(out.crlb_std_dev))

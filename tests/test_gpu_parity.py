@@ -114,7 +114,7 @@ def check_glrt_masks(nb, mean, var, hw, strides, nslc, alpha, label):
 
 def test_glrt_near_cutoff_is_exact():
     """Neighbours whose statistic sits 1e-9 .. 1e-4 (relative) from the cutoff: every
-    GPU decision is the exact one, where the float32 evaluation flips some."""
+    GPU decision is the exact one."""
     from scipy import stats
 
     nslc, alpha = 20, 0.001
@@ -130,8 +130,9 @@ def test_glrt_near_cutoff_is_exact():
     mean = np.zeros_like(var)
     nb = dp.estimate_neighbors(halfwin_rowcol=(0, 1), mean=mean, var=var, nslc=nslc, alpha=alpha)
     near, near_diff, flipped = check_glrt_masks(nb, mean, var, (0, 1), (1, 1), nslc, alpha, "GLRT near the cutoff")
-    assert near > 0 and near_diff == 0  # exact even within 1e-6 of the cutoff
-    assert flipped > 0  # where the float32 arithmetic flips decisions
+    # exact even within 1e-6 of the cutoff (how many float32 evaluations flip depends on
+    # the host's float32 log; check_glrt_masks prints it)
+    assert near > 0 and near_diff == 0
 
 
 def test_glrt_window_larger_than_image():
