@@ -37,7 +37,7 @@ class PlParams(C.Structure):
         ("use_evd", _i), ("beta", _d), ("zero_correlation_threshold", _d),
         ("reference_idx", _i), ("mask_input_ps", _i), ("use_max_ps", _i), ("use_slc_amp", _i),
         ("baseline_lag", _i), ("first_real_slc_idx", _i), ("compute_crlb", _i), ("cov_form", _i),
-        ("solver_slots", _i), ("solver_lanes", _i),
+        ("solver_slots", _i), ("solver_lanes", _i), ("nonconverged_mode", _i),
     ]
 
 
@@ -48,7 +48,7 @@ class PlInputs(C.Structure):
 class PlOutputs(C.Structure):
     _fields_ = [
         ("cpx_phase", _p), ("temp_coh", _p), ("shp_counts", _p), ("eigenvalues", _p),
-        ("estimator", _p), ("crlb_std_dev", _p), ("closure_phases", _p),
+        ("estimator", _p), ("crlb_std_dev", _p), ("closure_phases", _p), ("nonconverged", _p),
     ]
 
 

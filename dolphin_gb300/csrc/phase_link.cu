@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(256) k_prep(const cfloat* __restrict__ slc, in
 }  // namespace dpl
 
 #include "solver.cuh"
+#include "eigh.cuh"
 
 namespace dpl {
 
@@ -253,6 +254,139 @@ __global__ void __launch_bounds__(256) k_pixel(PixArgs a) {
         } else {
             solve_pixel<NB, kLU>(a, p, m, lane);
         }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// k_eigh: the dense eigensolver for the listed non-converged pixels (eigh.cuh), one
+// warp per pixel, a persistent grid over the list
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(32) k_eigh(PixArgs a, EighLayout L) {
+    extern __shared__ __align__(16) unsigned char eigh_smem[];
+    const int lane = threadIdx.x;
+    cfloat* C = reinterpret_cast<cfloat*>(eigh_smem + L.off_C);
+    cfloat* A = reinterpret_cast<cfloat*>(eigh_smem + L.off_A);
+    cfloat* V = reinterpret_cast<cfloat*>(eigh_smem + L.off_V);
+    double* G = reinterpret_cast<double*>(eigh_smem + L.off_G);
+    cfloat* w = reinterpret_cast<cfloat*>(eigh_smem + L.off_w);
+    const int n = a.n, ld = L.ld, lag = a.baseline_lag;
+    const int count = *a.nc_count;
+    for (int idx = blockIdx.x; idx < count; idx += gridDim.x) {
+        const int64_t p = a.nc_list[idx];
+        __syncwarp();
+        // the coherence, normalised as the solvers read it
+        if (a.Cplanar) {
+            const float* src = a.Cplanar + p * n * n;
+            float* rv = reinterpret_cast<float*>(w);
+            for (int i = lane; i < n; i += 32) rv[i] = __frsqrt_rn(src[i]);
+            __syncwarp();
+            for (int i = lane; i < n; i += 32) {
+                const float f = rv[i] * rv[i];
+                C[i * ld + i] = cmake(f < 1e6f ? src[i] * f : 0.f, 0.f);
+            }
+            for (int r = 1; r < n; ++r) {
+                const int o = r * (r - 1) / 2;
+                for (int c = lane; c < r; c += 32) {
+                    const float f = rv[r] * rv[c];
+                    cfloat v = f < 1e6f ? cmake(src[n + 2 * (o + c)] * f, src[n + 2 * (o + c) + 1] * f)
+                                        : cmake(0.f, 0.f);
+                    if (lag > 0 && r - c >= lag) v = cmake(0.f, 0.f);
+                    C[r * ld + c] = v;
+                    C[c * ld + r] = cconj(v);
+                }
+            }
+        } else {
+            const cfloat* src = a.Cin + p * n * n;
+            for (int r = 0; r < n; ++r)
+                for (int c = lane; c <= r; c += 32) {
+                    cfloat v = src[r * n + c];
+                    if (lag > 0 && r - c >= lag) v = cmake(0.f, 0.f);
+                    C[r * ld + c] = v;
+                    C[c * ld + r] = cconj(v);
+                }
+        }
+        __syncwarp();
+        const bool evd = a.est[p] == 0;  // the estimator the solver chose
+        bool ok = true;
+        if (!evd) {
+            // |Gamma| + 1e-6 I inverted in double; A = |Gamma|^{-1} o C
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j < n; j += 32)
+                    G[i * n + j] = (double)s_gamma(a, C[i * ld + j], i == j) + (i == j ? 1e-6 : 0.0);
+            ok = e_inverse_spd(G, n, lane);
+            if (ok)
+                for (int i = 0; i < n; ++i)
+                    for (int j = lane; j < n; j += 32) A[i * ld + j] = cscale(C[i * ld + j], (float)G[i * n + j]);
+        } else {
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j < n; j += 32) {
+                    const cfloat c = C[i * ld + j];
+                    A[i * ld + j] = cscale(c, sqrtf(c.re * c.re + c.im * c.im));
+                }
+        }
+        __syncwarp();
+        if (ok) {
+            e_jacobi(A, V, n, ld, lane);
+            // EMI: the eigenvalue nearest the shift 0.99; EVD: the largest in magnitude
+            float best = INFINITY;
+            int bi = n;
+            for (int i = lane; i < n; i += 32) {
+                const float lam = A[i * ld + i].re;
+                const float score = evd ? -fabsf(lam) : fabsf(lam - 0.99f);
+                if (score < best) {
+                    best = score;
+                    bi = i;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob < best || (ob == best && oi < bi)) {
+                    best = ob;
+                    bi = oi;
+                }
+            }
+            if (bi < n) {
+                const float lambda = A[bi * ld + bi].re;
+                float s2 = 0.f;
+                for (int i = lane; i < n; i += 32) s2 += cabs2(V[i * ld + bi]);
+                s2 = warp_sum(s2);
+                const float scale = (evd ? 1.f : sqrtf((float)n)) / sqrtf(s2);
+                const cfloat rot = cconj(fphasor(V[a.ref_idx * ld + bi]));
+                __syncwarp();
+                for (int i = lane; i < n; i += 32) {
+                    const cfloat v = cmul(cscale(V[i * ld + bi], scale), rot);
+                    a.vout[p * n + i] = v;
+                    w[i] = fphasor(v);
+                }
+                __syncwarp();
+                // temporal coherence over pairs c < r, as the solvers compute it
+                float sre = 0.f, sim = 0.f;
+                int cnt = 0;
+                for (int r = 1; r < n; ++r)
+                    for (int c = lane; c < r; c += 32) {
+                        const cfloat u = fphasor(C[r * ld + c]);
+                        const cfloat t = cconj(cmulc(cmul(u, w[c]), w[r]));
+                        if (!cisnan(t)) {
+                            sre += t.re;
+                            sim += t.im;
+                            ++cnt;
+                        }
+                    }
+                sre = warp_sum(sre);
+                sim = warp_sum(sim);
+                cnt = warp_sum_int(cnt);
+                if (lane == 0) {
+                    const float fc = (float)cnt;
+                    const float tc = hypotf(sre / fc, sim / fc);
+                    a.tcoh[p] = isfinite(tc) ? tc : 0.f;
+                    a.eig[p] = lambda;
+                }
+            }
+        }
+        if (lane == 0 && a.nc_flag) a.nc_flag[p] = 1;
+        __syncwarp();
     }
 }
 
@@ -484,21 +618,44 @@ static dpl_status launch_pixel64(const PixArgs& a, cudaStream_t s) {
     return check_launch("k_pixel64");
 }
 
+// Dense eigensolver over the listed non-converged pixels: one-warp CTAs, a persistent
+// grid of up to 8 per SM (the list length is known only on the device).
+static dpl_status launch_eigh(const PixArgs& a, cudaStream_t s) {
+    const EighLayout L = make_eigh_layout(a.n);
+    if (L.bytes > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "eigensolver: shared memory exceeds the SM limit");
+    int dev = 0, sms = 0;
+    DPL_CUDA_TRY(cudaGetDevice(&dev));
+    DPL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DPL_CUDA_TRY(cudaFuncSetAttribute(k_eigh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes));
+    k_eigh<<<(unsigned)std::max(1, sms * 8), 32, L.bytes, s>>>(a, L);
+    return check_launch("k_eigh");
+}
+
+// Solve pass, then the LU pass over the pixels it lists (`fb`: a counter, then room
+// for every pixel index) and, with `nc` (the same shape), the dense eigensolver over
+// the pixels whose iteration missed its stopping rule.
 template <int MODE>
-static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr) {
+static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr, int* nc = nullptr) {
     if (a.npix == 0) return DPL_OK;
     if (MODE == kCovOnly) return launch_pixel_pass<MODE, false>(a, s);
     if (!fb) return fail(DPL_ERR_WORKSPACE, "solver: missing fallback list");
     DPL_CUDA_TRY(cudaMemsetAsync(fb, 0, sizeof(int), s));
     a.fb_count = fb;
     a.fb_list = fb + 64;
+    // non-converged pixels are listed (and solved again) only where the coherence is stored
+    a.nc_count = MODE == kSolveOnly && nc ? nc : nullptr;
+    a.nc_list = a.nc_count ? nc + 64 : nullptr;
+    if (!a.nc_count) a.nc_flag = nullptr;
+    if (a.nc_count) DPL_CUDA_TRY(cudaMemsetAsync(nc, 0, sizeof(int), s));
     dpl_status st = MODE == kSolveOnly && a.n <= 64 ? launch_solve_reg(a, s) : launch_pixel_pass<MODE, false>(a, s);
     if (st != DPL_OK) return st;
     PixArgs b = a;
     fill_pix_layout(b, a.n, 2 * a.hx + 1, true);
     b.list = a.fb_list;
     b.list_count = a.fb_count;
-    return launch_pixel_pass<MODE, true>(b, s);
+    st = launch_pixel_pass<MODE, true>(b, s);
+    if (st != DPL_OK || !a.nc_count) return st;
+    return launch_eigh(a, s);
 }
 
 // Tensor-core covariance: fills `Cg` (npix x n*n planar floats).
@@ -595,6 +752,7 @@ struct PlWorkspace {
     unsigned int* valid_bits;
     float* Cg;
     int* fb;
+    int* nc;
     uint8_t* flags;
     float* avgmag;
     cfloat* zt;
@@ -611,6 +769,7 @@ static size_t pl_workspace_layout(int64_t n, int64_t rows, int64_t cols, int sy,
     t.valid_bits = ws.take<unsigned int>(16);
     t.Cg = cov_form == 0 ? ws.take<float>(P * n * n) : nullptr;
     t.fb = ws.take<int>(P + 64);
+    t.nc = ws.take<int>(P + 64);
     t.flags = ws.take<uint8_t>(npix);
     t.avgmag = ws.take<float>(npix);
     t.zt = ws.take<cfloat>(npix * n);
@@ -658,6 +817,8 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
     const int ref = norm_ref(P.reference_idx, n);
     if (ref < 0 || ref >= n) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
     if (P.cov_form < 0 || P.cov_form > 2) return fail(DPL_ERR_INVALID_ARGUMENT, "cov_form must be 0, 1 or 2");
+    if (P.nonconverged_mode < 0 || P.nonconverged_mode > 1)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "nonconverged_mode must be 0 or 1");
     if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
     PlWorkspace w;
@@ -695,6 +856,9 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
         a.baseline_lag = P.baseline_lag > 0 ? P.baseline_lag : 0;
         a.slots = P.solver_slots;
         a.lanes = P.solver_lanes;
+        a.nc_flag = P.nonconverged_mode == 0 ? out->nonconverged : nullptr;
+        a.eigh = P.nonconverged_mode == 0;
+        if (out->nonconverged) DPL_CUDA_TRY(cudaMemsetAsync(out->nonconverged, 0, (size_t)Pout, s));
         a.vout = w.V;
         a.eig = out->eigenvalues;
         a.est = out->estimator;
@@ -715,7 +879,9 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
             });
             if (st != DPL_OK) return st;
             a.Cplanar = w.Cg;
-            st = timed(s, 1, [&] { return launch_pixel<kSolveOnly>(a, s, w.fb); });
+            st = timed(s, 1, [&] {
+                return launch_pixel<kSolveOnly>(a, s, w.fb, P.nonconverged_mode == 0 ? w.nc : nullptr);
+            });
         } else {
             // plain form (or a window too large for the tensor-core tiles): SIMT covariance
             // fused with the solver

@@ -79,6 +79,10 @@ struct PixArgs {
     const int* list;         // LU pass: pixels list[0 .. *list_count)
     const int* list_count;
     int lanes;               // register solver: threads per pixel (8, 16, 32; 0 = the smallest that fits)
+    int* nc_list;            // pixels whose eigen-iteration missed its stopping rule (null: not listed)
+    int* nc_count;
+    uint8_t* nc_flag;        // (npix) 1 where the dense eigensolver replaced the iterate, or null
+    int eigh;                // FP64 form: the dense eigensolver for iterations that miss the rule
     int slots;               // register solver: row slots K (even, >= n; 0 = n rounded up to even)
 };
 

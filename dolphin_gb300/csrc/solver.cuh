@@ -295,9 +295,10 @@ __device__ void s_publish(cfloat* vpub, const cfloat (&x)[NB], int n, int lane) 
     __syncwarp();
 }
 
-// Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps.
+// Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps; true
+// if the stopping rule was met.
 template <int NB, class Op>
-__device__ void s_iterate(cfloat (&v)[NB], Op&& op) {
+__device__ bool s_iterate(cfloat (&v)[NB], Op&& op) {
     float diff = 1.f;
     for (int it = 1; diff > 1e-5f && it < 50; ++it) {
         cfloat x[NB];
@@ -315,6 +316,7 @@ __device__ void s_iterate(cfloat (&v)[NB], Op&& op) {
         }
         diff = sqrtf(warp_sum(dd));
     }
+    return !(diff > 1e-5f);  // a NaN difference ends the loop too, as in the reference
 }
 
 // Full solve for one pixel whose packed coherence matrix is in m.C.  With kLU the
@@ -362,6 +364,7 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
 #pragma unroll
     for (int q = 0; q < NB; ++q) v[q] = lane + 32 * q < n ? cmake(inv_sqrt_n, 0.f) : cmake(0.f, 0.f);
     float lambda;
+    bool converged;
     if (!evd) {
         if (!kLU) {
             // packed A - 0.99 I, complex Cholesky, inverse iteration
@@ -377,7 +380,7 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
                 __syncwarp();
                 return;
             }
-            s_iterate<NB>(v, [&](cfloat(&x)[NB]) { s_chol_solve<NB>(m.R, m.d, n, x, lane); });
+            converged = s_iterate<NB>(v, [&](cfloat(&x)[NB]) { s_chol_solve<NB>(m.R, m.d, n, x, lane); });
             s_publish<NB>(m.v, v, n, lane);
             float s = 0.f;
 #pragma unroll
@@ -412,7 +415,7 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
                 }
             }
             __syncwarp();
-            s_iterate<NB>(v, [&](cfloat(&x)[NB]) { s_lu_solve<NB>(A, n, src, x, lane); });
+            converged = s_iterate<NB>(v, [&](cfloat(&x)[NB]) { s_lu_solve<NB>(A, n, src, x, lane); });
             s_publish<NB>(m.v, v, n, lane);
             float s = 0.f;
 #pragma unroll
@@ -436,7 +439,7 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
             m.R[e] = cscale(c, sqrtf(c.re * c.re + c.im * c.im));
         }
         __syncwarp();
-        s_iterate<NB>(v, [&](cfloat(&x)[NB]) {
+        converged = s_iterate<NB>(v, [&](cfloat(&x)[NB]) {
             s_publish<NB>(m.v, x, n, lane);
             s_hermv<NB>(m.R, n, m.v, x, lane);
         });
@@ -482,6 +485,8 @@ __device__ void solve_pixel(const PixArgs& a, int64_t p, const SolveMats& m, int
     if (lane == 0) {
         a.eig[p] = lambda;
         a.est[p] = evd ? 0 : 1;
+        // the stopping rule not met within 49 steps: listed for the dense eigensolver
+        if (!converged && a.nc_list) a.nc_list[atomicAdd(a.nc_count, 1)] = (int)p;
     }
     // temporal coherence over pairs i < j: phasor(C_ij) conj(phasor(v_i conj v_j)),
     // with C_ij = conj(C_ji) (packed (j, i)) and phasor(v_i conj v_j) = w_i conj(w_j)

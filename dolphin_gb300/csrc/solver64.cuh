@@ -57,7 +57,7 @@ __device__ __forceinline__ cdbl dphasor(cdbl c) {
 
 struct Pix64Layout {
     int ldg;
-    size_t off_C, off_G, off_A, off_v, off_piv, bytes;
+    size_t off_C, off_G, off_A, off_V, off_v, off_piv, bytes;
 };
 
 inline Pix64Layout make_layout64(int n, int stg) {
@@ -72,6 +72,7 @@ inline Pix64Layout make_layout64(int n, int stg) {
     L.off_C = take((size_t)n * (n + 1) / 2 * sizeof(cdbl));
     L.off_G = take((size_t)n * L.ldg * sizeof(double));
     L.off_A = take(std::max((size_t)n * n * sizeof(cdbl), (size_t)stg * sizeof(cfloat)));
+    L.off_V = take((size_t)n * n * sizeof(cdbl));
     L.off_v = take(64 * sizeof(cdbl));
     L.off_piv = take(128 * sizeof(int));
     L.bytes = align_up(o, 128);
@@ -296,7 +297,7 @@ __device__ void hermv64(const cdbl* H, int n, const cdbl* vpub, cdbl (&y)[NB], i
 }
 
 template <int NB, class Op>
-__device__ void iterate64(cdbl (&v)[NB], Op&& op) {
+__device__ bool iterate64(cdbl (&v)[NB], Op&& op) {
     double diff = 1.0;
     for (int it = 1; diff > 1e-5 && it < 50; ++it) {
         cdbl x[NB];
@@ -313,6 +314,103 @@ __device__ void iterate64(cdbl (&v)[NB], Op&& op) {
         }
         diff = sqrt(dwarp_sum(dd));
     }
+    return !(diff > 1e-5);  // a NaN difference ends the loop too, as in the reference
+}
+
+// The dense eigensolver of the non-convergence fallback (eigh.cuh) in double: cyclic
+// Jacobi on the Hermitian A (n x n, both triangles), eigenvectors in the columns of V,
+// eigenvalues on the diagonal of A.
+__device__ inline void e_jacobi64(cdbl* A, cdbl* V, int n, int lane) {
+    for (int i = 0; i < n; ++i)
+        for (int j = lane; j < n; j += 32) V[i * n + j] = dmk(i == j ? 1.0 : 0.0, 0.0);
+    __syncwarp();
+    for (int sweep = 0; sweep < kEighMaxSweeps; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = lane; j < n; j += 32) {
+                const double m2 = dabs2(A[i * n + j]);
+                tot += m2;
+                if (j != i) off += m2;
+            }
+        off = dwarp_sum(off);
+        tot = dwarp_sum(tot);
+        if (!(off > 1e-30 * tot)) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const cdbl b = A[p * n + q];
+                const double e = sqrt(dabs2(b));
+                if (!(e > 0.0)) continue;
+                const double a = A[p * n + p].re, d = A[q * n + q].re;
+                const double zeta = (d - a) / (2.0 * e);
+                const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+                const cdbl ph = dmk(b.re / e, b.im / e);
+                const cdbl sm = dmk(s * ph.re, -s * ph.im);
+                const cdbl cm = dmk(c * ph.re, -c * ph.im);
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) {
+                    const cdbl xp = A[k * n + p], xq = A[k * n + q];
+                    A[k * n + p] = dsub(dscale(xp, c), dmul(sm, xq));
+                    A[k * n + q] = dadd(dscale(xp, s), dmul(cm, xq));
+                    const cdbl vp = V[k * n + p], vq = V[k * n + q];
+                    V[k * n + p] = dsub(dscale(vp, c), dmul(sm, vq));
+                    V[k * n + q] = dadd(dscale(vp, s), dmul(cm, vq));
+                }
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) {
+                    const cdbl xp = A[p * n + k], xq = A[q * n + k];
+                    A[p * n + k] = dsub(dscale(xp, c), dmul(dconj(sm), xq));
+                    A[q * n + k] = dadd(dscale(xp, s), dmul(dconj(cm), xq));
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    A[p * n + q] = dmk(0.0, 0.0);
+                    A[q * n + p] = dmk(0.0, 0.0);
+                    A[p * n + p] = dmk(a - t * e, 0.0);
+                    A[q * n + q] = dmk(d + t * e, 0.0);
+                }
+                __syncwarp();
+            }
+    }
+    __syncwarp();
+}
+
+// The fallback's choice on diag(A) after e_jacobi64: EMI the eigenvalue nearest 0.99,
+// EVD the largest in magnitude; v (lane i + 32 q holds entry i) gets that column of V
+// at unit norm, and the eigenvalue is returned.
+template <int NB>
+__device__ double pick64(const cdbl* A, const cdbl* V, int n, bool evd, cdbl (&v)[NB], int lane) {
+    double best = INFINITY;
+    int bi = n;
+    for (int i = lane; i < n; i += 32) {
+        const double lam = A[i * n + i].re;
+        const double score = evd ? -fabs(lam) : fabs(lam - 0.99);
+        if (score < best) {
+            best = score;
+            bi = i;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob < best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+        }
+    }
+    if (bi >= n) bi = 0;
+    double s2 = 0.0;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        const int i = lane + 32 * q;
+        v[q] = i < n ? V[i * n + bi] : dmk(0.0, 0.0);
+        s2 += dabs2(v[q]);
+    }
+    const double inv = 1.0 / sqrt(dwarp_sum(s2));
+#pragma unroll
+    for (int q = 0; q < NB; ++q) v[q] = dscale(v[q], inv);
+    return A[bi * n + bi].re;
 }
 
 __device__ __forceinline__ double gamma64(const PixArgs& a, cdbl c, bool diag) {
@@ -322,8 +420,8 @@ __device__ __forceinline__ double gamma64(const PixArgs& a, cdbl c, bool diag) {
 }
 
 template <int NB>
-__device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld, cdbl* A, cdbl* vp, int* piv,
-                        int lane) {
+__device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld, cdbl* A, cdbl* V, cdbl* vp,
+                        int* piv, int lane) {
     const int n = a.n;
     if (a.baseline_lag > 0) {
         for (int i = a.baseline_lag; i < n; ++i)
@@ -357,6 +455,7 @@ __device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld,
 #pragma unroll
     for (int q = 0; q < NB; ++q) v[q] = lane + 32 * q < n ? dmk(inv_sqrt_n, 0.0) : dmk(0.0, 0.0);
     double lambda;
+    bool converged;
     if (!evd) {
         for (int i = 0; i < n; ++i)
             for (int j = lane; j < n; j += 32) {
@@ -376,7 +475,7 @@ __device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld,
             }
         }
         __syncwarp();
-        iterate64<NB>(v, [&](cdbl(&x)[NB]) { lusolve64<NB>(A, n, src, x, lane); });
+        converged = iterate64<NB>(v, [&](cdbl(&x)[NB]) { lusolve64<NB>(A, n, src, x, lane); });
         publish64<NB>(vp, v, n, lane);
         double s = 0.0;
 #pragma unroll
@@ -389,6 +488,14 @@ __device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld,
             }
         }
         lambda = dwarp_sum(s);
+        if (!converged && a.eigh) {
+            // the dense eigensolver on A = |Gamma|^{-1} o C (the LU factors are no longer needed)
+            __syncwarp();
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j < n; j += 32) A[i * n + j] = dscale(dget(C, i, j), G[i * ld + j]);
+            e_jacobi64(A, V, n, lane);
+            lambda = pick64<NB>(A, V, n, false, v, lane);
+        }
         const double scale = sqrt((double)n) / sqrt(d_norm2<NB>(v));
 #pragma unroll
         for (int q = 0; q < NB; ++q) v[q] = dscale(v[q], scale);
@@ -396,7 +503,7 @@ __device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld,
         const int T = tri(n);
         for (int e = lane; e < T; e += 32) A[e] = dscale(C[e], sqrt(dabs2(C[e])));
         __syncwarp();
-        iterate64<NB>(v, [&](cdbl(&x)[NB]) {
+        converged = iterate64<NB>(v, [&](cdbl(&x)[NB]) {
             publish64<NB>(vp, x, n, lane);
             hermv64<NB>(A, n, vp, x, lane);
         });
@@ -407,6 +514,20 @@ __device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld,
 #pragma unroll
         for (int q = 0; q < NB; ++q) s += v[q].re * y[q].re + v[q].im * y[q].im;
         lambda = dwarp_sum(s);
+        if (!converged && a.eigh) {
+            // the dense eigensolver on the full C o |C|
+            __syncwarp();
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j < n; j += 32) {
+                    const cdbl c = dget(C, i, j);
+                    V[i * n + j] = dscale(c, sqrt(dabs2(c)));
+                }
+            __syncwarp();
+            for (int i = 0; i < n; ++i)
+                for (int j = lane; j < n; j += 32) A[i * n + j] = V[i * n + j];
+            e_jacobi64(A, V, n, lane);
+            lambda = pick64<NB>(A, V, n, true, v, lane);
+        }
     }
     __syncwarp();
     if (a.compute_crlb) {
@@ -440,6 +561,7 @@ __device__ void solve64(const PixArgs& a, int64_t p, cdbl* C, double* G, int ld,
     if (lane == 0) {
         a.eig[p] = (float)lambda;
         a.est[p] = evd ? 0 : 1;
+        if (a.nc_flag) a.nc_flag[p] = !converged && a.eigh ? 1 : 0;
     }
     cdbl w[NB];
 #pragma unroll
@@ -477,13 +599,14 @@ __global__ void __launch_bounds__(128) k_pixel64(PixArgs a, Pix64Layout L) {
     cdbl* C = reinterpret_cast<cdbl*>(base + L.off_C);
     double* G = reinterpret_cast<double*>(base + L.off_G);
     cdbl* A = reinterpret_cast<cdbl*>(base + L.off_A);
+    cdbl* V = reinterpret_cast<cdbl*>(base + L.off_V);
     cdbl* vp = reinterpret_cast<cdbl*>(base + L.off_v);
     int* piv = reinterpret_cast<int*>(base + L.off_piv);
     for (int64_t p = (int64_t)blockIdx.x * nwarps + warp; p < a.npix; p += (int64_t)gridDim.x * nwarps) {
         int count = 0;
         cov64<NB>(a, p, C, reinterpret_cast<cfloat*>(A), reinterpret_cast<double*>(vp), lane, &count);
         if (a.counts && lane == 0) a.counts[p] = count;
-        solve64<NB>(a, p, C, G, L.ldg, A, vp, piv, lane);
+        solve64<NB>(a, p, C, G, L.ldg, A, V, vp, piv, lane);
     }
 }
 

@@ -231,9 +231,9 @@ __device__ __forceinline__ void r_prefetch(float* dst, const float* src, int cou
 
 // Normalising iteration x <- op(v) / |op(v)| until |x - v| <= 1e-5 or 49 steps
 // (the reference's while-loop: iteration count starts at 1, stops below 50).  Adds the
-// steps taken to `steps`; returns whether the stopping rule was met.
+// steps taken to `steps`; returns the last step's difference (NaN also ends the loop).
 template <int G, class Op>
-__device__ __forceinline__ bool r_iterate(cfloat& v, const Grp<G>& gr, int& steps, Op&& op) {
+__device__ __forceinline__ float r_iterate(cfloat& v, const Grp<G>& gr, int& steps, Op&& op) {
     float diff = 1.f;
     for (int it = 1; diff > 1e-5f && it < 50; ++it) {
         cfloat x = op(v);
@@ -243,7 +243,7 @@ __device__ __forceinline__ bool r_iterate(cfloat& v, const Grp<G>& gr, int& step
         v = x;
         ++steps;
     }
-    return diff <= 1e-5f;
+    return diff;
 }
 
 // Full solve for one pixel whose Hermitian coherence matrix is in Cf (n x ld, both
@@ -364,10 +364,14 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
             warm = true;
         }
     }
-    if (!r_iterate<G>(v, gr, steps, op) && warm) {
+    float diff = r_iterate<G>(v, gr, steps, op);
+    if (!(diff <= 1e-5f) && warm) {  // a warm start that misses the rule (or goes NaN): plain EMI
         v = row ? cmake(1.f / sqrtf((float)n), 0.f) : cmake(0.f, 0.f);
-        r_iterate<G>(v, gr, steps, op);
+        diff = r_iterate<G>(v, gr, steps, op);
     }
+    // 49 steps without meeting the stopping rule (a NaN difference stops the loop, as in
+    // the reference): listed for the dense eigensolver
+    if (diff > 1e-5f && a.nc_list && me == 0) a.nc_list[atomicAdd(a.nc_count, 1)] = (int)p;
     if (!evd) {
         // lambda = Re v^H A v, A_ij = |Gamma|^{-1}_ij C_ij
         gr.sync();

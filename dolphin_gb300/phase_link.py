@@ -120,6 +120,8 @@ def run_phase_linking(
     covariance_form: str = "tensor",
     solver_slots: int = 0,
     solver_lanes: int = 0,
+    eigh_fallback: bool = True,
+    nonconverged=None,
 ) -> PhaseLinkOutput:
     """Estimate the linked phase for a stack of SLCs (phase_link/_core.py:67-249).
 
@@ -136,6 +138,12 @@ def run_phase_linking(
     register solver's row slots (even, >= N) and threads per pixel (8, 16, 32); 0 picks
     the smallest that fit.  A tuner's choices (``dolphin_gb300.tune_forms``); the results
     are the same.
+
+    ``eigh_fallback`` (keyword-only, not in the reference): pixels whose eigen-iteration
+    misses the stopping rule within 49 steps are solved again by a dense Hermitian
+    eigensolver (tensor-core form); ``False`` keeps the last iterate, as the reference
+    does.  ``nonconverged``: an optional (rows', cols') uint8 array (a CUDA tensor for
+    device inputs) that receives 1 on those pixels.
     """
     on_device = D.is_device_tensor(slc_stack)
     shape = tuple(slc_stack.shape)
@@ -176,6 +184,7 @@ def run_phase_linking(
         baseline_lag=int(baseline_lag) if baseline_lag else 0,
         first_real_slc_idx=int(first_real_slc_idx), compute_crlb=int(bool(compute_crlb)),
         cov_form=_form_code(covariance_form), solver_slots=int(solver_slots), solver_lanes=int(solver_lanes),
+        nonconverged_mode=0 if eigh_fallback else 1,
     )
     cpx = D.empty((nslc, out_rows, out_cols), np.complex64)
     tcoh = D.empty((out_rows, out_cols), np.float32)
@@ -188,9 +197,14 @@ def run_phase_linking(
     ws = D.workspace(lib.dpl_phase_link_workspace_size(prm))
     inp = _lib.PlInputs(slc=D.ptr(slc), nodata_mask=D.ptr(nodata), ps_mask=D.ptr(ps), neighbors=D.ptr(nb),
                         avg_mag=D.ptr(am))
+    ncflag = None
+    if nonconverged is not None:
+        if tuple(nonconverged.shape) != (out_rows, out_cols):
+            raise ValueError(f"nonconverged.shape={tuple(nonconverged.shape)} != {(out_rows, out_cols)}")
+        ncflag = D.empty((out_rows, out_cols), np.uint8)
     outp = _lib.PlOutputs(cpx_phase=D.ptr(cpx), temp_coh=D.ptr(tcoh), shp_counts=D.ptr(counts),
                           eigenvalues=D.ptr(eig), estimator=D.ptr(est), crlb_std_dev=D.ptr(crlb),
-                          closure_phases=D.ptr(clos) if nslc > 2 else None)
+                          closure_phases=D.ptr(clos) if nslc > 2 else None, nonconverged=D.ptr(ncflag))
     pending = getattr(_deferred, "pending", None) if on_device else None
     if pending is None:
         st = lib.dpl_phase_link(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle())
@@ -205,6 +219,11 @@ def run_phase_linking(
         event = torch.cuda.Event()
         event.record()
         pending.append((nslc, words, event))
+    if ncflag is not None:
+        if D.is_device_tensor(nonconverged):
+            nonconverged.copy_(ncflag)
+        else:
+            nonconverged[...] = D.to_host(ncflag)
     if on_device:
         if counts is None:
             counts = D.require_cuda().zeros((out_rows, out_cols), dtype=D.torch().int16, device=cpx.device)

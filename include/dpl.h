@@ -128,6 +128,13 @@ typedef struct dpl_pl_params {
      * reductions may round differently. */
     int solver_slots;
     int solver_lanes;
+    /* Not in the reference.  Pixels whose eigen-iteration misses the stopping rule within
+     * 49 steps (the reference returns that last iterate, _eigenvalues.py:194-202):
+     * 0 (default) -- solved again by a dense Hermitian eigensolver (|Gamma| inverted in
+     * double precision, cyclic Jacobi) and flagged in outputs->nonconverged; 1 -- keep
+     * the last iterate, as the reference does.  Applies to the tensor-core form (the
+     * forms that store the coherence). */
+    int nonconverged_mode;
 } dpl_pl_params;
 
 typedef struct dpl_pl_inputs {
@@ -146,6 +153,8 @@ typedef struct dpl_pl_outputs {
     uint8_t* estimator;            /* (out_rows, out_cols) uint8: 0 EVD, 1 EMI */
     float* crlb_std_dev;           /* (nslc, out_rows, out_cols) float32 */
     float* closure_phases;         /* (out_rows, out_cols, nslc - 2) float32; may be NULL */
+    uint8_t* nonconverged;         /* (out_rows, out_cols) uint8 or NULL (not in the reference): 1 where the
+                                      dense eigensolver replaced an iterate that missed the stopping rule */
 } dpl_pl_outputs;
 
 size_t dpl_phase_link_workspace_size(const dpl_pl_params* params);

@@ -491,8 +491,9 @@ def _norm(v):
     return np.sqrt(np.sum((v.real * v.real + v.imag * v.imag), axis=-1))
 
 
-def power_iteration(A, tol=1e-5, max_iters=50):
-    """phase_link/_eigenvalues.py:93-136, batched over pixels (A: (B, n, n))."""
+def power_iteration(A, tol=1e-5, max_iters=50, return_active=False):
+    """phase_link/_eigenvalues.py:93-136, batched over pixels (A: (B, n, n)); with
+    ``return_active`` also the pixels that missed the stopping rule."""
     bsz, n, _ = A.shape
     cdt = A.dtype
     v = np.ones((bsz, n), dtype=cdt)
@@ -510,10 +511,12 @@ def power_iteration(A, tol=1e-5, max_iters=50):
             active[idx[~still]] = False
             iters += 1
         lam = np.einsum("bi,bij,bj->b", np.conj(v), A, v)
+    if return_active:
+        return lam.real, v, active
     return lam.real, v
 
 
-def inverse_iteration(A, mu, tol=1e-5, max_iters=50):
+def inverse_iteration(A, mu, tol=1e-5, max_iters=50, return_active=False):
     """phase_link/_eigenvalues.py:139-205, batched over pixels."""
     bsz, n, _ = A.shape
     cdt = A.dtype
@@ -534,7 +537,21 @@ def inverse_iteration(A, mu, tol=1e-5, max_iters=50):
             active[idx[~still]] = False
             iters += 1
         lam = np.einsum("bi,bij,bj->b", np.conj(v), A, v)
+    if return_active:
+        return lam.real, v, active
     return lam.real, v
+
+
+def eigh_fallback_vectors(A, target):
+    """The fallback for pixels whose eigen-iteration missed its stopping rule (not in the
+    reference): the eigenvector of the Hermitian A (B, n, n), in float64, whose eigenvalue
+    is nearest 0.99 (``target="emi"``, the shifted inverse iteration's limit) or largest in
+    magnitude (``"evd"``, power iteration's limit); returns (eigenvalues, unit vectors)."""
+    A64 = np.asarray(A).astype(np.complex128)
+    w, V = np.linalg.eigh(A64)
+    k = np.argmin(np.abs(w - 0.99), axis=-1) if target == "emi" else np.argmax(np.abs(w), axis=-1)
+    b = np.arange(A64.shape[0])
+    return w[b, k], V[b, :, k]
 
 
 def _crlb(gamma, gamma_inv, num_looks, ref, fim_jitter=1e-6):
@@ -556,16 +573,19 @@ def _crlb(gamma, gamma_inv, num_looks, ref, fim_jitter=1e-6):
 
 def process_coherence_matrices(C, use_evd=False, beta=0.0, zero_correlation_threshold=0.0,
                                reference_idx=0, num_looks=1.0, first_real_slc_idx=0,
-                               compute_crlb=True):
+                               compute_crlb=True, eigh_fallback=False, nonconverged=None):
     """phase_link/_core.py:379-534 on a batch of matrices C: (B, n, n).
 
     Returns (referenced eigenvector (B, n), eigenvalue (B,), estimator (B,) uint8,
-    crlb (B, n)).
+    crlb (B, n)).  ``eigh_fallback`` (not in the reference): pixels whose iteration for
+    the chosen estimator missed the stopping rule get the float64 dense eigenvector
+    (``eigh_fallback_vectors``; for EMI with |Gamma| inverted in float64); their mask is
+    written to ``nonconverged`` (a (B,) bool array) when given.
     """
     C = np.asarray(C)
     bsz, n, _ = C.shape
     rdt = C.real.dtype
-    evd_vals, evd_vecs = power_iteration(C * np.abs(C))
+    evd_vals, evd_vecs, evd_active = power_iteration(C * np.abs(C), return_active=True)
     gamma = np.abs(C)
     eye = np.eye(n, dtype=rdt)
     if beta > 0:
@@ -573,17 +593,37 @@ def process_coherence_matrices(C, use_evd=False, beta=0.0, zero_correlation_thre
     gamma = np.where(gamma < zero_correlation_threshold, rdt.type(0), gamma)
     L = _cholesky_lower(gamma + rdt.type(1e-6) * eye)
     gamma_inv = _cho_inverse(L)
+    if eigh_fallback and evd_active.any():
+        w, V = eigh_fallback_vectors((C * np.abs(C))[evd_active], "evd")
+        evd_vals = evd_vals.copy()
+        evd_vecs = evd_vecs.copy()
+        evd_vals[evd_active] = w
+        evd_vecs[evd_active] = V.astype(C.dtype)
     if use_evd:
         vals, vecs = evd_vals, evd_vecs
         estimator = np.zeros(bsz, dtype=np.uint8)
+        active = evd_active
     else:
-        emi_vals, emi_vecs = inverse_iteration((gamma_inv * C).astype(C.dtype), 0.99)
+        emi_vals, emi_vecs, emi_active = inverse_iteration((gamma_inv * C).astype(C.dtype), 0.99,
+                                                           return_active=True)
+        bad = np.any(np.isnan(gamma_inv), axis=(-1, -2))
+        fix = emi_active & ~bad
+        if eigh_fallback and fix.any():
+            g64 = gamma[fix].astype(np.float64) + 1e-6 * np.eye(n)
+            A64 = np.linalg.inv(g64) * C[fix].astype(np.complex128)
+            w, V = eigh_fallback_vectors(A64, "emi")
+            emi_vals = emi_vals.copy()
+            emi_vecs = emi_vecs.copy()
+            emi_vals[fix] = w
+            emi_vecs[fix] = V.astype(C.dtype)
         with np.errstate(all="ignore"):
             emi_vecs = (np.sqrt(rdt.type(n)) * emi_vecs / _norm(emi_vecs)[:, None]).astype(C.dtype)
-        bad = np.any(np.isnan(gamma_inv), axis=(-1, -2))
         vecs = np.where(bad[:, None], evd_vecs, emi_vecs)
         vals = np.where(bad, evd_vals, emi_vals)
         estimator = np.where(bad, 0, 1).astype(np.uint8)
+        active = np.where(bad, evd_active, emi_active)
+    if nonconverged is not None:
+        nonconverged[...] = active
     if compute_crlb:
         crlb = _crlb(gamma, gamma_inv, num_looks, max(first_real_slc_idx - 1, 0))
     else:
@@ -700,10 +740,11 @@ def gamma_min_eig(C, beta=0.0, zero_correlation_threshold=0.0):
 def run_cpl(slc_stack, half_window, strides, use_evd=False, beta=0.0,
             zero_correlation_threshold=0.0, reference_idx=0, neighbor_arrays=None,
             baseline_lag=None, first_real_slc_idx=0, compute_crlb=True, dtype=np.float32,
-            chunk=2048, diagnostics=None):
+            chunk=2048, diagnostics=None, eigh_fallback=False):
     """phase_link/_core.py:252-376 (pixel-chunked so C is never held whole).
 
-    ``diagnostics`` (a dict, optional) receives ``gamma_min_eig`` per output pixel.
+    ``diagnostics`` (a dict, optional) receives ``gamma_min_eig`` and ``nonconverged``
+    (the iteration missed its stopping rule) per output pixel.
     """
     slc = np.asarray(slc_stack).astype(_cdt(dtype), copy=False)
     n, rows, cols = slc.shape
@@ -725,6 +766,7 @@ def run_cpl(slc_stack, half_window, strides, use_evd=False, beta=0.0,
     if baseline_lag:
         ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
         lag_zero = np.abs(ii - jj) >= baseline_lag
+    ncv = np.zeros(npx, bool)
     if diagnostics is not None:
         diagnostics["gamma_min_eig"] = np.zeros((out_rows, out_cols), np.float64)
     for s in range(0, npx, chunk):
@@ -739,9 +781,12 @@ def run_cpl(slc_stack, half_window, strides, use_evd=False, beta=0.0,
         v, lam, e, cr = process_coherence_matrices(
             C, use_evd=use_evd, beta=beta, zero_correlation_threshold=zero_correlation_threshold,
             reference_idx=reference_idx, num_looks=num_looks,
-            first_real_slc_idx=first_real_slc_idx, compute_crlb=compute_crlb)
+            first_real_slc_idx=first_real_slc_idx, compute_crlb=compute_crlb,
+            eigh_fallback=eigh_fallback, nonconverged=ncv[sl])
         cpx[sl], eig[sl], est[sl], crlb[sl] = v, lam, e, cr
         temp_coh[sl] = estimate_temp_coh(v, C)
+    if diagnostics is not None:
+        diagnostics["nonconverged"] = ncv.reshape(out_rows, out_cols)
     if neighbor_arrays is None:
         shp_counts = np.zeros((out_rows, out_cols), dtype=np.int16)
     else:
@@ -762,8 +807,9 @@ def run_phase_linking(slc_stack, half_window, strides=(1, 1), use_evd=False, bet
                       mask_input_ps=False, ps_mask=None, use_max_ps=True, neighbor_arrays=None,
                       avg_mag=None, use_slc_amp=False, baseline_lag=None,
                       first_real_slc_idx=0, compute_crlb=True, dtype=np.float32,
-                      diagnostics=None):
-    """phase_link/_core.py:67-249 (``diagnostics``: see :func:`run_cpl`)."""
+                      diagnostics=None, eigh_fallback=False):
+    """phase_link/_core.py:67-249 (``diagnostics``, ``eigh_fallback``: see :func:`run_cpl`
+    and :func:`process_coherence_matrices`)."""
     slc_stack = np.asarray(slc_stack)
     _, rows, cols = slc_stack.shape
     strides = tuple(strides)
@@ -787,7 +833,8 @@ def run_phase_linking(slc_stack, half_window, strides=(1, 1), use_evd=False, bet
                   zero_correlation_threshold=zero_correlation_threshold,
                   reference_idx=reference_idx, neighbor_arrays=neighbor_arrays,
                   baseline_lag=baseline_lag, first_real_slc_idx=first_real_slc_idx,
-                  compute_crlb=compute_crlb, dtype=dtype, diagnostics=diagnostics)
+                  compute_crlb=compute_crlb, dtype=dtype, diagnostics=diagnostics,
+                  eigh_fallback=eigh_fallback)
     mask_looked = take_looks(nodata_mask, *strides, func_type="all")
     temp_coh = np.array(cpl.temp_coh)
     cdt = _cdt(dtype)

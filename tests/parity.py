@@ -34,15 +34,36 @@ def judge_flips(out, ref, fp64, label="", tc_min=0.3, phase_tol=1e-3, tc_tol=1e-
     return flip
 
 
-def compare_pl(out, g, prefix, tc_min=0.3, phase_tol=1e-3, tc_tol=1e-4, fp64=None, label=None):
+def judge_nonconverged(out, flags, fp64, label="", tc_min=0.3, phase_tol=1e-3, tc_tol=1e-4):
+    """Pixels the dense eigensolver solved again (``flags``: the iteration missed its
+    stopping rule, where the reference returns its last iterate) are judged against the
+    FP64 answer ``fp64`` computed with the same fallback.  Returns the flag mask."""
+    f = np.zeros(out.temp_coh.shape, bool) if flags is None else np.asarray(flags).astype(bool)
+    if not f.any():
+        return f
+    assert fp64 is not None, f"{label}: {int(f.sum())} re-solved pixels and no FP64 answer to judge them"
+    fgood = f & (fp64.temp_coh > tc_min) & np.all(np.isfinite(fp64.cpx_phase), axis=0)
+    perr = phase_err(out.cpx_phase[:, fgood], fp64.cpx_phase[:, fgood].astype(np.complex64)) if fgood.any() else np.zeros(1)
+    terr = np.abs(out.temp_coh[fgood] - fp64.temp_coh[fgood]) if fgood.any() else np.zeros(1)
+    print(f"{label}: {int(f.sum())} pixels solved by the dense eigensolver; on the {int(fgood.sum())} coherent "
+          f"ones: phase error vs FP64 {float(perr.max()):.2e} rad, coherence {float(terr.max()):.2e}")
+    assert perr.max() <= phase_tol, perr.max()
+    assert terr.max() <= tc_tol, terr.max()
+    return f
+
+
+def compare_pl(out, g, prefix, tc_min=0.3, phase_tol=1e-3, tc_tol=1e-4, fp64=None, label=None, nonconverged=None):
     """Compare a PhaseLinkOutput with golden outputs ``{prefix}_{field}`` in ``g``.
 
     Pixels whose EMI-vs-EVD choice differs from the golden one (|Gamma| within rounding
-    of singular) are judged against the FP64 answer ``fp64`` (see ``judge_flips``) and
+    of singular) are judged against the FP64 answer ``fp64`` (see ``judge_flips``), and
+    so are the pixels flagged in ``nonconverged`` (``judge_nonconverged``); both are
     left out of the comparison with the golden outputs.
     """
     ref = {k: g[f"{prefix}_{k}"] for k in O.PhaseLinkOutput._fields}
     borderline = judge_flips(out, O.PhaseLinkOutput(**ref), fp64, label or str(prefix), tc_min, phase_tol, tc_tol)
+    borderline = borderline | judge_nonconverged(out, nonconverged, fp64, label or str(prefix), tc_min, phase_tol,
+                                                 tc_tol)
     if borderline.any():
         keep = ~borderline
         ref = {k: (v[..., keep] if k in ("cpx_phase", "crlb_std_dev") else v[keep]) if v.ndim >= 2 else v

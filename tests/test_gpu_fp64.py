@@ -4,7 +4,8 @@ Both compute in double; the GPU writes float32 outputs, so phases agree to float
 rounding (~1e-7 rad) and the temporal coherence to ~1e-7.  Pixels whose |Gamma| +
 1e-6 I has a smallest eigenvalue below 1e-9 (where even double rounding decides the
 Cholesky outcome) are left out of the estimator comparison; eigenvalues and CRLB are
-compared where C has full rank.
+compared where C has full rank.  Both solve the pixels whose iteration misses the
+stopping rule again with a dense eigensolver in double (the default of both).
 """
 
 import numpy as np
@@ -48,17 +49,29 @@ def test_fp64_precision_case():
     mean, disp, _ps = dp.calc_ps_block(np.abs(z), 0.25, cfg.nslc)
     nb = dp.estimate_neighbors(halfwin_rowcol=hw, alpha=0.001, mean=mean, var=(disp * mean) ** 2, nslc=cfg.nslc)
     diag = {}
-    ref = O.run_phase_linking(z, hw, neighbor_arrays=nb, dtype=np.float64, diagnostics=diag)
-    out = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form="fp64")
+    ref = O.run_phase_linking(z, hw, neighbor_arrays=nb, dtype=np.float64, diagnostics=diag, eigh_fallback=True)
+    flags = np.zeros(z.shape[1:], np.uint8)
+    out = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form="fp64", nonconverged=flags)
     np.testing.assert_array_equal(out.shp_counts, ref.shp_counts)
+    np.testing.assert_array_equal(flags.astype(bool), diag["nonconverged"])
     _compare(out, ref, diag, ref.shp_counts >= cfg.nslc)
-    # the float32 forms against it: the precision table's denominator on the GPU
-    for form in ("tensor", "simt"):
-        o32 = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form=form)
-        good = (out.temp_coh > 0.3) & (diag["gamma_min_eig"] >= 1e-3)
-        err = phase_err(o32.cpx_phase[:, good], out.cpx_phase[:, good])
-        print(f"[fp64] form={form:6s} vs GPU float64: phase err max {err.max():.2e} rad on {good.sum()} pixels")
-        assert err.max() < 1e-3
+    # the float32 forms against it: the precision table's denominator on the GPU.  The
+    # SIMT form (fused, the coherence never stored) keeps the last iterate: it is compared
+    # with the FP64 form doing the same.
+    last = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form="fp64", eigh_fallback=False)
+    for form, ref_form in (("tensor", out), ("simt", last)):
+        f32 = np.zeros(z.shape[1:], np.uint8)
+        o32 = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form=form, nonconverged=f32)
+        good = (ref_form.temp_coh > 0.3) & (diag["gamma_min_eig"] >= 1e-3)
+        err = phase_err(o32.cpx_phase[:, good], ref_form.cpx_phase[:, good]).max(0)
+        above = err > 1e-3
+        differ = (f32.astype(bool) != flags.astype(bool))[good]
+        print(f"[fp64] form={form:6s} vs GPU float64: phase err max {err.max():.2e} rad on {good.sum()} pixels, "
+              f"{int(above.sum())} above 1e-3 ({int((above & differ).sum())} of them where only one of the two "
+              f"forms met the stopping rule); {int(f32.sum())} / {int(flags.sum())} dense-eigensolver pixels")
+        # slowly converging pixels (contraction near 1 per step) carry the stopping rule's
+        # own error, |step| / (1 - ratio), up to ~1e-3 rad in either form
+        assert err.max() < 2e-3 and above.mean() <= 1e-3
 
 
 @pytest.mark.parametrize("kw", [
@@ -81,7 +94,7 @@ def test_fp64_options_against_oracle(kw):
                                nslc=cfg.nslc)
     diag = {}
     ref = O.run_phase_linking(z, hw, strides, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, dtype=np.float64,
-                              diagnostics=diag, **kw)
+                              diagnostics=diag, eigh_fallback=True, **kw)
     out = dp.run_phase_linking(z, hw, strides, ps_mask=ps, neighbor_arrays=nb, avg_mag=mean,
                                covariance_form="fp64", **kw)
     np.testing.assert_array_equal(out.shp_counts, ref.shp_counts)

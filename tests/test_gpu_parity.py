@@ -320,19 +320,22 @@ def test_run_phase_linking_golden_cases(golden, form):
             if key in kw:
                 kw[key] = np.array(g[kw[key]])
         okw = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in kw.items()}
-        ref64 = O.run_phase_linking(np.array(g[zname]), hw, strides, dtype=np.float64, **okw)
-        out = dp.run_phase_linking(np.array(g[zname]), hw, strides, covariance_form=form, **kw)
-        compare_pl(out, g, idx, fp64=ref64, label=f"golden case {idx} ({form})")
+        ref64 = O.run_phase_linking(np.array(g[zname]), hw, strides, dtype=np.float64, eigh_fallback=True, **okw)
+        z = np.array(g[zname])
+        flags = np.zeros((z.shape[1] // strides[0], z.shape[2] // strides[1]), np.uint8)
+        out = dp.run_phase_linking(z, hw, strides, covariance_form=form, nonconverged=flags, **kw)
+        compare_pl(out, g, idx, fp64=ref64, label=f"golden case {idx} ({form})", nonconverged=flags)
 
 
 @pytest.mark.parametrize("form", ["tensor", "simt"])
 def test_config1_crop_golden(golden, form):
     g = golden("config1_crop")
     ref64 = O.run_phase_linking(g["slc"], (5, 5), (1, 1), ps_mask=g["ps"].copy(), neighbor_arrays=g["nb"],
-                                avg_mag=g["mean"], dtype=np.float64)
+                                avg_mag=g["mean"], dtype=np.float64, eigh_fallback=True)
+    flags = np.zeros(g["slc"].shape[1:], np.uint8)
     out = dp.run_phase_linking(g["slc"], (5, 5), ps_mask=g["ps"], neighbor_arrays=g["nb"], avg_mag=g["mean"],
-                               covariance_form=form)
-    compare_pl(out, g, "emi", fp64=ref64, label=f"config-1 crop ({form})")
+                               covariance_form=form, nonconverged=flags)
+    compare_pl(out, g, "emi", fp64=ref64, label=f"config-1 crop ({form})", nonconverged=flags)
 
 
 @pytest.mark.parametrize("strides", [1, 2, 3, 4, 5])
