@@ -11,7 +11,9 @@
 //             window and is an SHP of p (the B operand, N = 256 pixels; exact in bf16)
 //
 // KR is split into bf16 hi + lo parts (x = hi + lo + O(2^-17 x)); both products
-// accumulate into one fp32 accumulator in tensor memory.  A pass fills two M tiles
+// accumulate into one fp32 accumulator in tensor memory.  The TF32 form (kTf) stores KR
+// once, rounded to tf32 (x (1 + O(2^-11))), with a tf32 mask, and issues kind::tf32
+// MMAs (8 samples each); its stages are 64 KB, so two of them fit.  A pass fills two M tiles
 // (2 x 256 TMEM columns) row by row: in pass 0 rows 0 .. N-1 of M tile 0 hold the
 // diagonal; every other used row holds one lower pair, its real part in M tile 0 and
 // its imaginary part in the same row of M tile 1, so one builder thread forms both
@@ -52,7 +54,13 @@ constexpr int kTcThreads = 576;              // 18 warps
 constexpr int kTcBuilders = 544;             // warps 0-16; warp 17 issues the MMAs
 static_assert(4 * kTcRows <= kTcBuilders, "one Khatri-Rao item per builder");
 constexpr int kTcCols = 512;                 // TMEM columns: two M tiles x 256 pixels
-constexpr int kTcStageBytes = 4 * 8192 + 16384;  // KR hi/lo of two M tiles + mask
+constexpr int kTcStageBytes = 4 * 8192 + 16384;  // KR hi/lo of two M tiles + mask (bf16)
+// TF32 form: one tf32 plane per M tile (16 KB) and a tf32 mask (32 KB)
+constexpr int kTcStageBytesTf = 2 * 16384 + 32768;
+template <bool kTf>
+constexpr int tc_stage_bytes() {
+    return kTf ? kTcStageBytesTf : kTcStageBytes;
+}
 constexpr int kTcMaxStages = 3;
 
 struct TcArgs {
@@ -79,6 +87,28 @@ constexpr int kTcZBuf = 4;  // ring of chunk sample buffers (bulk prefetch dista
 // byte offset of element (row, k) in a K-major no-swizzle tile with KC columns
 __device__ __forceinline__ int tc_off(int row, int k) {
     return (row >> 3) * (kTcKC / 8 * 128) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+// byte offset of element (row, k) in a K-major no-swizzle tf32 tile with KC columns
+// (core matrices of 8 rows x 4 elements)
+__device__ __forceinline__ int tc_off32(int row, int k) {
+    return (row >> 3) * (kTcKC / 4 * 128) + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4;
+}
+
+// 8 values rounded to tf32 (nearest, ties away: cvt.rna.tf32.f32) into row `row`,
+// samples kb..kb+7, of a tf32 KR M tile
+__device__ __forceinline__ void tc_store8_tf32(unsigned char* plane, int row, int kb, const float (&x)[8]) {
+    uint32_t t[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t[q]) : "f"(x[q]));
+    *reinterpret_cast<uint4*>(plane + tc_off32(row, kb)) = make_uint4(t[0], t[1], t[2], t[3]);
+    *reinterpret_cast<uint4*>(plane + tc_off32(row, kb + 4)) = make_uint4(t[4], t[5], t[6], t[7]);
+}
+
+// 4 mask bits -> 4 tf32 (1.0 or 0)
+__device__ __forceinline__ uint4 tc_expand4_tf32(uint32_t b) {
+    return make_uint4((b & 1u) * 0x3F800000u, ((b >> 1) & 1u) * 0x3F800000u, ((b >> 2) & 1u) * 0x3F800000u,
+                      ((b >> 3) & 1u) * 0x3F800000u);
 }
 
 // bf16 hi/lo split of two values, packed (first value in the low half)
@@ -162,7 +192,9 @@ __device__ __forceinline__ void tc_prefetch_bulk(const TcArgs& a, cfloat* zs, ui
     }
 }
 
+template <bool kTf>
 __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
+    constexpr int kStage = tc_stage_bytes<kTf>();
     extern __shared__ unsigned char tc_raw[];
     // 1024-byte aligned base, derived from the shared array itself so that every access
     // below stays a shared-memory access
@@ -313,8 +345,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 if (!bulk) tc_prefetch(a, zbuf(0), soff, 0, btid);
                 for (int ch = 0, s = 0; ch < nchunks; ++ch, s = s + 1 == a.nst ? 0 : s + 1) {
                     const int zi = ch & (kTcZBuf - 1);
-                    unsigned char* stage = sm + a.off_stage + s * kTcStageBytes;
-                    unsigned char* msk = stage + 4 * 8192;
+                    unsigned char* stage = sm + a.off_stage + s * kStage;
+                    unsigned char* msk = stage + 32768;  // after the two M tiles in both forms
                     // Before building, the MMAs that last read this stage must be done and
                     // the chunk's samples must have landed.  Even N (bulk copies): each
                     // warp's lane 0 waits on the mbarriers and the warp reconverges, so the
@@ -361,16 +393,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                             xr[q] = fmaf(zi.re, zj.re, zi.im * zj.im);
                             xi[q] = fmaf(zi.im, zj.re, -(zi.re * zj.im));
                         }
-                        tc_store8(stage, stage + 8192, u, kb, xr);
-                        tc_store8(stage + 16384, stage + 24576, u, kb, xi);
+                        if (kTf) {
+                            tc_store8_tf32(stage, u, kb, xr);
+                            tc_store8_tf32(stage + 16384, u, kb, xi);
+                        } else {
+                            tc_store8(stage, stage + 8192, u, kb, xr);
+                            tc_store8(stage + 16384, stage + 24576, u, kb, xi);
+                        }
                     }
                     int m = btid - nkr;
                     if (m < 0) m += kTcBuilders;
                     for (; m < 2 * kTcN; m += kTcBuilders) {
                         const int row = m >> 1, half = m & 1;
                         const uint32_t bw = pbits[row * a.kwords + ch] >> (16 * half);
-                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(bw);
-                        *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(bw >> 8);
+                        if (kTf) {
+#pragma unroll
+                            for (int g4 = 0; g4 < 4; ++g4)
+                                *reinterpret_cast<uint4*>(msk + tc_off32(row, 16 * half + 4 * g4)) =
+                                    tc_expand4_tf32(bw >> (4 * g4));
+                        } else {
+                            *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half)) = tc_expand8(bw);
+                            *reinterpret_cast<uint4*>(msk + tc_off(row, 16 * half + 8)) = tc_expand8(bw >> 8);
+                        }
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
@@ -390,14 +434,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                 }
             } else if (lane == 0) {
                 // MMA issuer
-                constexpr uint32_t LBO = 128, SBO = kTcKC / 8 * 128;
-                const uint32_t idesc = tc_idesc_bf16(kTcM, kTcN);
+                // core matrices are 16 bytes wide: 8 bf16 or 4 tf32 samples
+                constexpr int kCoreK = kTf ? 4 : 8;
+                constexpr uint32_t LBO = 128, SBO = kTcKC / kCoreK * 128;
+                const uint32_t idesc = kTf ? tc_idesc_tf32(kTcM, kTcN) : tc_idesc_bf16(kTcM, kTcN);
                 // Descriptors of stage 0 (M tile 0, hi plane, k = 0) and of its mask.  Every
                 // other operand of a chunk lies a fixed offset away, and bits 0-13 of a
                 // descriptor hold the shared address >> 4: with every address below 256 KB,
                 // adding offset >> 4 never carries into the other fields.
                 const uint64_t dA = tc_desc(tc_smem(sm + a.off_stage), LBO, SBO);
-                const uint64_t dB = dA + (uint64_t)((4 * 8192) >> 4);
+                const uint64_t dB = dA + (uint64_t)(32768 >> 4);
                 if (bulk)
                     for (int c = 0; c < kTcZBuf && c < nchunks; ++c) arm_bulk(c, c);
                 for (int ch = 0, s = 0; ch < nchunks; ++ch, s = s + 1 == a.nst ? 0 : s + 1) {
@@ -407,18 +453,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
                     }
                     ph_full ^= 1u << s;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint64_t so = (uint64_t)((s * kTcStageBytes) >> 4);
+                    const uint64_t so = (uint64_t)((s * kStage) >> 4);
 #pragma unroll
                     for (int t = 0; t < 2; ++t) {
                         if (t >= mt) break;
                         const uint32_t dt = tmem + (uint32_t)(t * kTcN);
+                        // one MMA covers 32 bytes of K: 16 bf16 or 8 tf32 samples
 #pragma unroll
-                        for (int kk = 0; kk < kTcKC; kk += 16) {
-                            const uint64_t ko = (uint64_t)(((kk / 8) * LBO) >> 4);
+                        for (int kk = 0; kk < kTcKC; kk += 2 * kCoreK) {
+                            const uint64_t ko = (uint64_t)(((kk / kCoreK) * LBO) >> 4);
                             const uint64_t bd = dB + so + ko;
                             const uint64_t ah = dA + so + (uint64_t)((t * 16384) >> 4) + ko;
                             const uint64_t al = ah + (uint64_t)(8192 >> 4);
                             const uint32_t acc0 = (ch > 0 || kk > 0) ? 1u : 0u;
+                            if (kTf) {  // tf32: one product
+                                asm volatile(
+                                    "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+                                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+                                    "l"(ah), "l"(bd), "r"(idesc), "r"(acc0));
+                                continue;
+                            }
                             asm volatile(
                                 "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),

@@ -661,7 +661,7 @@ static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr, in
 // Tensor-core covariance: fills `Cg` (npix x n*n planar floats).
 // Tile, pass and shared-memory plan of the tensor-core covariance.  False if the
 // shape does not fit (then the plain SIMT form is used).
-static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, int sy, int sx) {
+static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, int sy, int sx, bool tf32 = false) {
     a.n = n;
     a.rows = rows;
     a.cols = cols;
@@ -692,7 +692,7 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
             o += bytes;
             return (int)at;
         };
-        a.off_stage = take((size_t)a.nst * kTcStageBytes, 1024);
+        a.off_stage = take((size_t)a.nst * (tf32 ? kTcStageBytesTf : kTcStageBytes), 1024);
         a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
         a.off_z = take(kTcZBuf * (size_t)a.z_bytes, 16);
         a.off_pbits = take((size_t)kTcN * a.kwords * sizeof(uint32_t), 16);
@@ -708,9 +708,10 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
 
 static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int sy, int sx, const cfloat* zt,
                                 const uint32_t* bits, int wpr, const uint8_t* nb_u8, float* Cg, int32_t* counts,
-                                int* status, cudaStream_t s) {
+                                int* status, cudaStream_t s, bool tf32 = false) {
     TcArgs a{};
-    if (!tc_configure(a, n, rows, cols, hy, hx, sy, sx)) return fail(DPL_ERR_UNSUPPORTED, "tensor-core covariance: unsupported shape");
+    if (!tc_configure(a, n, rows, cols, hy, hx, sy, sx, tf32))
+        return fail(DPL_ERR_UNSUPPORTED, "tensor-core covariance: unsupported shape");
     if (a.out_rows == 0 || a.out_cols == 0) return DPL_OK;
     a.zt = zt;
     a.bits = bits;
@@ -722,10 +723,15 @@ static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int s
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes));
     const int ntiles = a.tiles_r * a.tiles_c;
     const int grid = std::max(1, std::min(ntiles, sms));
-    k_cov_tc<<<grid, kTcThreads, a.smem_bytes, s>>>(a);
+    if (tf32) {
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes));
+        k_cov_tc<true><<<grid, kTcThreads, a.smem_bytes, s>>>(a);
+    } else {
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes));
+        k_cov_tc<false><<<grid, kTcThreads, a.smem_bytes, s>>>(a);
+    }
     return check_launch("k_cov_tc");
 }
 
@@ -767,7 +773,7 @@ static size_t pl_workspace_layout(int64_t n, int64_t rows, int64_t cols, int sy,
     PlWorkspace t{};
     t.status = ws.take<int>(16);
     t.valid_bits = ws.take<unsigned int>(16);
-    t.Cg = cov_form == 0 ? ws.take<float>(P * n * n) : nullptr;
+    t.Cg = cov_form == 0 || cov_form == 3 ? ws.take<float>(P * n * n) : nullptr;
     t.fb = ws.take<int>(P + 64);
     t.nc = ws.take<int>(P + 64);
     t.flags = ws.take<uint8_t>(npix);
@@ -816,7 +822,7 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
     const int n = (int)P.nslc;
     const int ref = norm_ref(P.reference_idx, n);
     if (ref < 0 || ref >= n) return fail(DPL_ERR_INVALID_ARGUMENT, "reference_idx out of range");
-    if (P.cov_form < 0 || P.cov_form > 2) return fail(DPL_ERR_INVALID_ARGUMENT, "cov_form must be 0, 1 or 2");
+    if (P.cov_form < 0 || P.cov_form > 3) return fail(DPL_ERR_INVALID_ARGUMENT, "cov_form must be 0, 1, 2 or 3");
     if (P.nonconverged_mode < 0 || P.nonconverged_mode > 1)
         return fail(DPL_ERR_INVALID_ARGUMENT, "nonconverged_mode must be 0 or 1");
     if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
@@ -867,7 +873,9 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
         a.closure = n > 2 ? out->closure_phases : nullptr;
         a.counts = in->neighbors ? out->shp_counts : nullptr;
         TcArgs tcfit{};
-        const bool tc_fits = P.cov_form == 0 && tc_configure(tcfit, n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx);
+        const bool tf32 = P.cov_form == 3;
+        const bool tc_fits = (P.cov_form == 0 || tf32) &&
+                             tc_configure(tcfit, n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, tf32);
         if (P.cov_form == 2) {
             // FP64 form: covariance and solver in double precision
             st = timed(s, 0, [&] { return launch_pixel64(a, s); });
@@ -875,7 +883,7 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
             // chosen form: tensor-core covariance, then the solver on the planar matrices
             st = timed(s, 0, [&] {
                 return launch_cov_tc(n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, w.zt, nullptr, 0,
-                                     in->neighbors, w.Cg, a.counts, w.status, s);
+                                     in->neighbors, w.Cg, a.counts, w.status, s, tf32);
             });
             if (st != DPL_OK) return st;
             a.Cplanar = w.Cg;
@@ -1005,8 +1013,8 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
                                      void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
     dpl_status st = validate_common(nslc, rows, cols, hy, hx, sy, sx);
     if (st != DPL_OK) return st;
-    if (cov_form != 0 && cov_form != 1)
-        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: cov_form must be 0 or 1 (2, fp64, is a phase-linking form)");
+    if (cov_form != 0 && cov_form != 1 && cov_form != 3)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: cov_form must be 0, 1 or 3 (2, fp64, is a phase-linking form)");
     if (!slc || !C || !workspace) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_covariance: null pointer");
     if (misaligned_c8(slc) || misaligned_c8(C) || (reinterpret_cast<uintptr_t>(workspace) & 15u))
         return fail(DPL_ERR_INVALID_ARGUMENT,
@@ -1043,10 +1051,11 @@ extern "C" dpl_status dpl_covariance(const float* slc, int64_t nslc, int64_t row
     a.nb_u8 = neighbors;
     a.Cout = reinterpret_cast<cfloat*>(C);
     TcArgs tcfit{};
-    if (cov_form == 1 || !tc_configure(tcfit, n, (int)rows, (int)cols, hy, hx, sy, sx))
+    if (cov_form == 1 || !tc_configure(tcfit, n, (int)rows, (int)cols, hy, hx, sy, sx, cov_form == 3))
         return launch_pixel<kCovOnly>(a, s);
     DPL_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
-    st = launch_cov_tc(n, (int)rows, (int)cols, hy, hx, sy, sx, zt, nullptr, 0, neighbors, Cg, nullptr, status, s);
+    st = launch_cov_tc(n, (int)rows, (int)cols, hy, hx, sy, sx, zt, nullptr, 0, neighbors, Cg, nullptr, status, s,
+                       cov_form == 3);
     if (st != DPL_OK) return st;
     const int64_t tot = a.npix * n * n;
     k_unpack_planar<<<ceil_div(tot, 256), 256, 0, s>>>(Cg, n, a.npix, reinterpret_cast<cfloat*>(C));

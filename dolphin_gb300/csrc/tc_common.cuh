@@ -29,6 +29,17 @@ __device__ __forceinline__ uint32_t tc_idesc_bf16(int m, int nn) {
     return d;
 }
 
+// kind::tf32 with tf32 A and B (format code 2 in both fields) and an fp32 accumulator
+__device__ __forceinline__ uint32_t tc_idesc_tf32(int m, int nn) {
+    uint32_t d = 0;
+    d |= 1u << 4;   // D: f32
+    d |= 2u << 7;   // A: tf32
+    d |= 2u << 10;  // B: tf32
+    d |= (uint32_t)(nn >> 3) << 17;
+    d |= (uint32_t)(m >> 4) << 24;
+    return d;
+}
+
 __device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // one test of an mbarrier phase with a suspend-time hint: the thread is suspended

@@ -130,7 +130,8 @@ def run_phase_linking(
 
     ``covariance_form`` (keyword-only, not in the reference): ``"tensor"`` computes
     the coherence matrices on the tensor cores (bf16 hi/lo split, fp32
-    accumulation); ``"simt"`` uses fp32 CUDA-core arithmetic throughout; ``"fp64"``
+    accumulation); ``"tf32"`` the same contraction with tf32 operands (one product,
+    fp32 accumulation); ``"simt"`` uses fp32 CUDA-core arithmetic throughout; ``"fp64"``
     computes the covariance and the solve in double precision (a reference form: GB300's
     FP64 rate is low), writing the same float32 outputs.
 
@@ -240,7 +241,7 @@ def run_phase_linking(
 
 
 def _form_code(form: str) -> int:
-    codes = {"tensor": 0, "simt": 1, "fp64": 2}
+    codes = {"tensor": 0, "simt": 1, "fp64": 2, "tf32": 3}
     if form not in codes:
         raise ValueError(f"covariance_form must be one of {sorted(codes)}, got {form!r}")
     return codes[form]

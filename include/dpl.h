@@ -120,8 +120,9 @@ typedef struct dpl_pl_params {
     int baseline_lag;              /* <= 0: off */
     int first_real_slc_idx;
     int compute_crlb;
-    int cov_form;                  /* 0: tensor-core covariance (default); 1: SIMT covariance (plain form);
-                                      2: covariance and solver in FP64 (the double-precision reference form) */
+    int cov_form;                  /* 0: tensor-core covariance, bf16 hi/lo (default); 1: SIMT covariance (plain
+                                      form); 2: covariance and solver in FP64 (the double-precision reference
+                                      form); 3: tensor-core covariance with tf32 operands (one product) */
     /* Not in the reference (zero = default).  Register-solver instance: row slots K (even,
      * >= nslc; 0 = nslc rounded up to even) and threads per pixel (8, 16 or 32 for K <= 32;
      * 0 = the smallest power of two >= K); a tuner's choices: the same algorithm, group

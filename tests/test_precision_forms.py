@@ -41,10 +41,10 @@ def case():
     r = np.arange(CFG.rows)[:, None] - CFG.rows / 2.0
     c = np.arange(CFG.cols)[None, :] - CFG.cols / 2.0
     disk = r * r + c * c <= (CFG.disk_radius * max(CFG.rows, CFG.cols)) ** 2
-    return z, nb, {"tensor": ref, "simt": ref_last}, diag, disk
+    return z, nb, {"tensor": ref, "tf32": ref, "simt": ref_last}, diag, disk
 
 
-@pytest.mark.parametrize("form", ["tensor", "simt"])
+@pytest.mark.parametrize("form", ["tensor", "simt", "tf32"])
 def test_precision_form_vs_float64(case, form):
     z, nb, refs, diag, disk = case
     ref = refs[form]
@@ -60,5 +60,9 @@ def test_precision_form_vs_float64(case, form):
     for name, npx, emax, e99, tmax in rows:
         print(f"[precision] form={form:6s} {name:8s} pixels={npx:5d} phase err max {emax:.2e} "
               f"p99 {e99:.2e} rad, temp_coh err max {tmax:.2e}")
+    if form == "tf32":
+        # one tf32 product per sample (11 significant bits): reported, with a looser bound
+        assert rows[-1][3] < 1e-3 and rows[-1][2] < 0.1
+        return
     assert rows[-1][2] < 1e-3
     assert rows[-1][4] < 1e-4
