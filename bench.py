@@ -618,7 +618,12 @@ def fp64_check(torch, dp, stack, entry):
 
 
 def run_precision(args):
-    """Rates of the two covariance forms on the precision workload (one GPU)."""
+    """The precision workload (N=40, 2048x2048, half-window (7, 7), gamma_inf 0.02 and a
+    high-coherence disk): rates of the covariance forms (tensor cores with bf16 hi/lo or
+    tf32 operands, SIMT), and on a 512x512 crop holding the disk's edge each form's error
+    against the FP64 GPU form, like with like (the SIMT form, whose coherence is never
+    stored, keeps the last iterate where the iteration misses its stopping rule, and is
+    compared with the FP64 form doing the same)."""
     import torch
 
     import dolphin_gb300 as dp
@@ -631,8 +636,9 @@ def run_precision(args):
                       disk_radius=0.125, ps_frac=0.0)
     stack = make_stack_torch(cfg)
     plan = block_plan(frame, frame, BLOCK, half)
+    forms = ("tensor", "tf32", "simt")
     rates = {}
-    for form in ("tensor", "simt"):
+    for form in forms:
         def step():
             for (ir, ic, *_r) in plan:
                 blk = stack[:, ir[0]:ir[1], ic[0]:ic[1]].contiguous()
@@ -649,36 +655,40 @@ def run_precision(args):
         e1.record()
         torch.cuda.synchronize()
         rates[form] = frame * frame * max(1, args.steps) / (e0.elapsed_time(e1) / 1000.0)
-    # the FP64 form (covariance and solver in double) on a 512x512 crop that holds the
-    # disk's edge: its rate, and each float32 form's error against it
     r0 = frame // 2 - 256 + int(0.125 * frame) // 2
     crop = stack[:, r0:r0 + 512 + 2 * half[0], r0:r0 + 512 + 2 * half[1]].contiguous()
     cm, cd, _cps = dp.calc_ps_block(crop.abs(), PS_THR, n)
     cnb = dp.estimate_neighbors(halfwin_rowcol=half, alpha=ALPHA, mean=cm, var=(cd * cm) ** 2, nslc=n)
-    outs, crop_rates = {}, {}
-    for form in ("fp64", "tensor", "simt"):
-        dp.run_phase_linking(crop, half, neighbor_arrays=cnb, covariance_form=form)
+    outs, crop_rates, flags = {}, {}, {}
+    for form in ("fp64", "fp64_last") + forms:
+        f = torch.zeros(crop.shape[1:], dtype=torch.uint8, device=crop.device)
+        kw = dict(covariance_form="fp64" if form.startswith("fp64") else form, eigh_fallback=form != "fp64_last",
+                  nonconverged=f)
+        dp.run_phase_linking(crop, half, neighbor_arrays=cnb, **kw)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        outs[form] = dp.run_phase_linking(crop, half, neighbor_arrays=cnb, covariance_form=form)
+        outs[form] = dp.run_phase_linking(crop, half, neighbor_arrays=cnb, **kw)
         e1.record()
         torch.cuda.synchronize()
         crop_rates[form] = crop.shape[1] * crop.shape[2] / (e0.elapsed_time(e1) / 1000.0)
-    ref = outs["fp64"]
-    good = ref.temp_coh > 0.3
+        flags[form] = int(f.sum())
     errs = {}
-    for form in ("tensor", "simt"):
+    for form in forms:
+        ref = outs["fp64_last" if form == "simt" else "fp64"]
+        good = ref.temp_coh > 0.3
         d = torch.angle(outs[form].cpx_phase[:, good] * ref.cpx_phase[:, good].conj()).abs()
         t = (outs[form].temp_coh[good] - ref.temp_coh[good]).abs()
         worst = d.max(0).values  # per pixel, over the SLCs
-        errs[form] = {"phase_max_rad": float(d.max()), "phase_p99_rad": float(torch.quantile(d.flatten()[:2**24], 0.99)),
-                      "pixels_above_1e-3_rad": int((worst > 1e-3).sum()), "temp_coh_max": float(t.max())}
+        errs[form] = {"phase_max_rad": float(worst.max()), "phase_p99_rad": float(torch.quantile(worst, 0.99)),
+                      "pixels_above_1e-3_rad": int((worst > 1e-3).sum()), "coherent_pixels": int(good.sum()),
+                      "temp_coh_max": float(t.max()), "dense_eigensolver_pixels": flags[form],
+                      "against": "fp64 with the same fallback" if form != "simt" else "fp64 keeping the last iterate"}
     print(json.dumps({"workload": "precision", "config": {"nslc": n, "frame": frame, "half_window": half,
                                                           "gamma_inf": 0.02, "disk_gamma0": 0.95},
                       "unit": UNIT, "rates": rates, "tensor_over_simt": rates["tensor"] / rates["simt"],
                       "fp64_crop": {"pixels": int(crop.shape[1] * crop.shape[2]), "rates": crop_rates,
-                                    "coherent_pixels": int(good.sum()), "errors_vs_fp64": errs}}),
+                                    "dense_eigensolver_pixels": flags, "errors_vs_fp64": errs}}),
           flush=True)
 
 
@@ -884,10 +894,14 @@ def run_batch(args):
         return e0.elapsed_time(e1) / reps
 
     reps = max(1, args.steps)
+    # persistent: one dpl_phase_link_batch (the covariance of all 12 stacks in one work-
+    # queue launch); per stack: one dpl_phase_link per stack; each eager and as a graph
     eager = PhaseLinkBatch(stacks, half, forms=forms, graph=False)
     eager_ms = timed(eager.run, reps)
     graph = PhaseLinkBatch(stacks, half, forms=forms, graph=True)
     graph_ms = timed(graph.run, reps)
+    per_stack = PhaseLinkBatch(stacks, half, forms=forms, graph=True, persistent=False)
+    per_stack_ms = timed(per_stack.run, reps)
     # per-ministack latency (eager, one stack per call)
     lat = []
     for _ in range(reps):
@@ -900,7 +914,10 @@ def run_batch(args):
                    "outlier_frac": 0.4, "ps_frac": 0.03},
         "forms": {str(k): v for k, v in forms.items()},
         "eager": px / (eager_ms / 1000.0), "graph": px / (graph_ms / 1000.0),
-        "ms_per_batch": {"eager": eager_ms, "graph": graph_ms},
+        "per_stack_graph": px / (per_stack_ms / 1000.0),
+        "ms_per_batch": {"eager": eager_ms, "graph": graph_ms, "per_stack_graph": per_stack_ms},
+        "note": "eager and graph: the persistent path (dpl_phase_link_batch); per_stack_graph: one dpl_phase_link "
+                "per stack in one graph; ministack_ms: each stack alone",
         "ministack_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
     }), flush=True)
 

@@ -67,6 +67,9 @@ SIGNATURES = {
     "dpl_phase_link_status": (_i, [C.POINTER(PlParams), _p, _sz, _p]),
     "dpl_phase_link_status_copy": (_i, [C.POINTER(PlParams), _p, _sz, _p, _p]),
     "dpl_phase_link_status_words": (_i, [_i64, _p]),
+    "dpl_phase_link_batch_workspace_size": (_sz, [C.POINTER(PlParams), _i]),
+    "dpl_phase_link_batch": (_i, [C.POINTER(PlParams), C.POINTER(PlInputs), C.POINTER(PlOutputs), _i, _p, _sz, _p]),
+    "dpl_phase_link_batch_status": (_i, [C.POINTER(PlParams), _i, _p, _sz, _p]),
     "dpl_covariance_workspace_size": (_sz, [_i64, _i64, _i64]),
     "dpl_covariance": (_i, [_p, _i64, _i64, _i64, _i, _i, _i, _i, _p, _i, _p, _p, _sz, _p]),
     "dpl_process_coherence_workspace_size": (_sz, [_i64]),

@@ -131,13 +131,17 @@ def _choice(forms, n):
 class PhaseLinkBatch:
     """PS + GLRT + phase linking over a list of (N_k, rows, cols) complex64 CUDA stacks.
 
-    Parameters follow ``run_phase_linking`` (EMI/EVD, CRLB, references) and
+    With ``persistent`` (the default) the whole batch is one ``dpl_phase_link_batch``
+    call: the tensor-core covariance of every stack is one persistent launch over a
+    work queue of (stack, tile) items, largest N first; ``persistent=False`` enqueues one
+    ``dpl_phase_link`` per stack.  Parameters follow ``run_phase_linking`` (EMI/EVD,
+    CRLB, references) and
     ``estimate_neighbors`` (GLRT ``alpha``); ``forms`` maps N to a ``tune_forms`` entry
     or to a bare covariance form, "tensor" or "simt" (default: ``tune_forms``).  ``graph=False`` runs every call eagerly.
     """
 
     def __init__(self, stacks, half_window, strides=(1, 1), alpha=0.001, ps_threshold=0.25, use_evd=False,
-                 compute_crlb=True, reference_idx=0, forms=None, graph=True):
+                 compute_crlb=True, reference_idx=0, forms=None, graph=True, persistent=True):
         self.stacks = list(stacks)
         for z in self.stacks:
             if not (D.is_device_tensor(z) and z.is_complex() and z.dim() == 3 and z.is_contiguous()):
@@ -149,6 +153,9 @@ class PhaseLinkBatch:
         depths = [int(z.shape[0]) for z in self.stacks]
         self.forms = dict(forms) if forms is not None else tune_forms(depths, self.hw, self.st)
         self.graph_enabled = bool(graph)
+        self.persistent = bool(persistent)
+        if self.persistent and len(self.stacks) > 16:
+            raise ValueError("a persistent batch takes at most 16 stacks")
         self._graph = None
         self._outs = None
         self._calls = None  # per stack: (params, workspace tensor)
@@ -181,26 +188,44 @@ class PhaseLinkBatch:
                 "crlb": torch.empty((n, orow, ocol), dtype=torch.float32, device=z.device),
                 "clos": torch.empty((orow, ocol, max(n - 2, 1)), dtype=torch.float32, device=z.device),
             }
-            ws = torch.empty(max(int(lib.dpl_phase_link_workspace_size(prm)), 256), dtype=torch.uint8,
-                             device=z.device)
             inp = _lib.PlInputs(slc=D.ptr(z), nodata_mask=None, ps_mask=D.ptr(ps), neighbors=D.ptr(nb),
                                 avg_mag=D.ptr(mean))
             outp = _lib.PlOutputs(cpx_phase=D.ptr(o["cpx"]), temp_coh=D.ptr(o["tc"]), shp_counts=D.ptr(o["cnt"]),
                                   eigenvalues=D.ptr(o["eig"]), estimator=D.ptr(o["est"]),
                                   crlb_std_dev=D.ptr(o["crlb"]),
                                   closure_phases=D.ptr(o["clos"]) if n > 2 else None)
-            _lib.check(lib.dpl_phase_link_async(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle()),
-                       "dpl_phase_link_async")
             o["_keep"] = (mean, disp, ps, nb)  # inputs of the captured kernels stay allocated
             outs.append(o)
-            calls.append((prm, ws))
-        return outs, calls
+            calls.append((prm, inp, outp))
+        if self.persistent:
+            # one dpl_phase_link_batch: the covariance of every stack in one work-queue launch
+            k = len(calls)
+            prms = (_lib.PlParams * k)(*[c[0] for c in calls])
+            inps = (_lib.PlInputs * k)(*[c[1] for c in calls])
+            outps = (_lib.PlOutputs * k)(*[c[2] for c in calls])
+            nbytes = int(lib.dpl_phase_link_batch_workspace_size(prms, k))
+            ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.stacks[0].device)
+            _lib.check(lib.dpl_phase_link_batch(prms, inps, outps, k, D.ptr(ws), ws.numel(), D.stream_handle()),
+                       "dpl_phase_link_batch")
+            return outs, [("batch", prms, k, ws)]
+        out_calls = []
+        for prm, inp, outp in calls:
+            ws = torch.empty(max(int(lib.dpl_phase_link_workspace_size(prm)), 256), dtype=torch.uint8,
+                             device=self.stacks[0].device)
+            _lib.check(lib.dpl_phase_link_async(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle()),
+                       "dpl_phase_link_async")
+            out_calls.append(("one", prm, 1, ws))
+        return outs, out_calls
 
     def _check(self, calls):
         lib = _lib.load()
-        for prm, ws in calls:
-            _lib.check(lib.dpl_phase_link_status(prm, D.ptr(ws), ws.numel(), D.stream_handle()),
-                       "dpl_phase_link")
+        for kind, prm, k, ws in calls:
+            if kind == "batch":
+                _lib.check(lib.dpl_phase_link_batch_status(prm, k, D.ptr(ws), ws.numel(), D.stream_handle()),
+                           "dpl_phase_link_batch")
+            else:
+                _lib.check(lib.dpl_phase_link_status(prm, D.ptr(ws), ws.numel(), D.stream_handle()),
+                           "dpl_phase_link")
 
     def run(self):
         """Process every stack; returns a list of ``PhaseLinkOutput`` (CUDA tensors)."""

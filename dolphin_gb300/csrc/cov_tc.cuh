@@ -81,6 +81,14 @@ struct TcArgs {
     int off_stage, off_z, z_bytes, off_pbits, off_soff, off_runs, off_rows, off_bar, smem_bytes;
 };
 
+// A batch of stacks for one work-queue launch (passed as a kernel parameter, 2.6 KB).
+constexpr int kTcMaxItems = 16;
+struct TcBatch {
+    TcArgs items[kTcMaxItems];
+    int tile_start[kTcMaxItems];
+    int nitems, total;
+};
+
 constexpr int kTcRuns = 3;  // contiguous runs of image samples per K chunk (a chunk spans <= 3 region rows)
 constexpr int kTcZBuf = 4;  // ring of chunk sample buffers (bulk prefetch distance)
 
@@ -192,23 +200,31 @@ __device__ __forceinline__ void tc_prefetch_bulk(const TcArgs& a, cfloat* zs, ui
     }
 }
 
-template <bool kTf>
-__global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
+// One launch serves one stack (kQueue false: the tiles of b.items[0], strided over the
+// grid) or a batch of stacks (kQueue true): b.items[i] describes stack i, b.tile_start[i]
+// its first tile in the batch's tile numbering (b.total tiles in all), and every CTA
+// takes the next batch tile from `counter` (a work queue; the items are ordered largest
+// first).  All items share one shared-memory carve (offsets, stage count, z_bytes).
+template <bool kTf, bool kQueue>
+__global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(const __grid_constant__ TcBatch b, int* counter) {
     constexpr int kStage = tc_stage_bytes<kTf>();
     extern __shared__ unsigned char tc_raw[];
     // 1024-byte aligned base, derived from the shared array itself so that every access
     // below stays a shared-memory access
     unsigned char* sm = tc_raw + ((1024u - (tc_smem(tc_raw) & 1023u)) & 1023u);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n = a.n, nn = n * n, wy = 2 * a.hy + 1, wx = 2 * a.hx + 1;
-    const int O = n * (n - 1) / 2;
+    TcArgs a = b.items[0];
+    int cur = 0;  // the item `a` describes
+    int n = a.n, nn = n * n, wy = 2 * a.hy + 1, wx = 2 * a.hx + 1;
+    int O = n * (n - 1) / 2;
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + a.off_bar);  // [kTcMaxStages] builders -> issuer
     uint64_t* empty = full + kTcMaxStages;                           // [kTcMaxStages] MMAs done -> builders
     uint64_t* zbar = empty + kTcMaxStages;                           // [kTcZBuf] bulk sample copies landed
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(zbar + kTcZBuf);
     int* sfail = reinterpret_cast<int*>(tmem_slot + 2);
+    int* snext = sfail + 1;                                          // the next batch tile (kQueue)
     int2* runs = reinterpret_cast<int2*>(sm + a.off_runs);          // [nchunks][kTcRuns]
-    const bool bulk = (a.n & 1) == 0;
+    bool bulk = (a.n & 1) == 0;
     auto zbuf = [&](int c) { return reinterpret_cast<cfloat*>(sm + a.off_z + (c & (kTcZBuf - 1)) * a.z_bytes); };
     uint32_t* pbits = reinterpret_cast<uint32_t*>(sm + a.off_pbits);  // [256][kwords]: pixel mask bits
     int* soff = reinterpret_cast<int*>(sm + a.off_soff);              // [kpad]: sample offsets in zt
@@ -217,21 +233,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
 
     for (int e = tid; e < kTcZBuf * a.z_bytes / 4; e += kTcThreads)  // no NaN patterns in unused slots
         reinterpret_cast<float*>(sm + a.off_z)[e] = 0.f;
-    for (int idx = tid; idx < a.npass * kTcRows; idx += kTcThreads) {
-        const int pass = idx / kTcRows, u = idx - pass * kTcRows;
-        const int d0 = pass == 0 ? n : 0;
-        const int o = (pass == 0 ? 0 : (kTcRows - n) + (pass - 1) * kTcRows) + u - d0;
-        uint32_t ij = 0u;  // unused rows: (0, 0)
-        if (u < d0) {
-            ij = (uint32_t)u | ((uint32_t)u << 16);
-        } else if (o < O) {
-            int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j, 0 <= j < i
-            while (i * (i - 1) / 2 > o) --i;
-            while ((i + 1) * i / 2 <= o) ++i;
-            ij = (uint32_t)i | ((uint32_t)(o - i * (i - 1) / 2) << 16);
+    // the row table of the current item's N (rebuilt when a batch moves to another stack)
+    auto fill_rowtab = [&]() {
+        for (int idx = tid; idx < a.npass * kTcRows; idx += kTcThreads) {
+            const int pass = idx / kTcRows, u = idx - pass * kTcRows;
+            const int d0 = pass == 0 ? n : 0;
+            const int o = (pass == 0 ? 0 : (kTcRows - n) + (pass - 1) * kTcRows) + u - d0;
+            uint32_t ij = 0u;  // unused rows: (0, 0)
+            if (u < d0) {
+                ij = (uint32_t)u | ((uint32_t)u << 16);
+            } else if (o < O) {
+                int i = (int)((sqrtf(8.f * o + 1.f) + 1.f) * 0.5f);  // o = i(i-1)/2 + j, 0 <= j < i
+                while (i * (i - 1) / 2 > o) --i;
+                while ((i + 1) * i / 2 <= o) ++i;
+                ij = (uint32_t)i | ((uint32_t)(o - i * (i - 1) / 2) << 16);
+            }
+            rowtab[idx] = ij;
         }
-        rowtab[idx] = ij;
-    }
+    };
+    fill_rowtab();
     if (tid == 0) {
         for (int s = 0; s < a.nst; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&full[s])), "r"(kTcBuilders / 32));
@@ -264,10 +284,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cov_tc(TcArgs a) {
         z_arm ^= 1u << zi;
         z_used |= 1u << zi;
     };
-    const int nchunks = a.kpad / kTcKC;
+    int nchunks = a.kpad / kTcKC;
 
     const int ntiles = a.tiles_r * a.tiles_c;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int it = 0;; ++it) {
+        int tile;
+        if (kQueue) {
+            __syncthreads();  // the previous tile is done with every shared buffer and with snext
+            if (tid == 0) *snext = atomicAdd(counter, 1);
+            __syncthreads();
+            const int t = *snext;
+            if (t >= b.total) break;
+            int i = cur;  // a CTA's tiles only increase, so its item only moves forward
+            while (i + 1 < b.nitems && b.tile_start[i + 1] <= t) ++i;
+            if (i != cur) {
+                cur = i;
+                a = b.items[i];
+                n = a.n;
+                nn = n * n;
+                wy = 2 * a.hy + 1;
+                wx = 2 * a.hx + 1;
+                O = n * (n - 1) / 2;
+                bulk = (n & 1) == 0;
+                nchunks = a.kpad / kTcKC;
+                fill_rowtab();
+                __syncthreads();
+            }
+            tile = t - b.tile_start[i];
+        } else {
+            tile = blockIdx.x + it * gridDim.x;
+            if (tile >= ntiles) break;
+        }
         const int tr0 = (tile / a.tiles_c) * kTcTileR, tc0 = (tile % a.tiles_c) * kTcTileC;
         // region origin: clamped window start of the tile's first output pixel
         const int rr0 = min(max(a.sy / 2 + tr0 * a.sy - a.hy, 0), a.rows - wy);

@@ -661,6 +661,28 @@ static dpl_status launch_pixel(PixArgs& a, cudaStream_t s, int* fb = nullptr, in
 // Tensor-core covariance: fills `Cg` (npix x n*n planar floats).
 // Tile, pass and shared-memory plan of the tensor-core covariance.  False if the
 // shape does not fit (then the plain SIMT form is used).
+// Shared-memory carve of the covariance kernel for nst operand stages, sized for up to
+// n SLCs, kpad region samples and npass passes (a batch carves once for all its items).
+static void tc_carve(TcArgs& a, int nst, int n, int kpad, int npass, bool tf32) {
+    size_t o = 0;
+    auto take = [&](size_t bytes, size_t al) {
+        o = align_up(o, al);
+        size_t at = o;
+        o += bytes;
+        return (int)at;
+    };
+    a.nst = nst;
+    a.off_stage = take((size_t)nst * (tf32 ? kTcStageBytesTf : kTcStageBytes), 1024);
+    a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
+    a.off_z = take(kTcZBuf * (size_t)a.z_bytes, 16);
+    a.off_pbits = take((size_t)kTcN * (kpad / 32) * sizeof(uint32_t), 16);
+    a.off_soff = take((size_t)kpad * sizeof(int), 16);
+    a.off_runs = take((size_t)(kpad / kTcKC) * kTcRuns * sizeof(int2), 16);
+    a.off_rows = take((size_t)npass * kTcRows * sizeof(uint32_t), 16);
+    a.off_bar = take(128, 64);
+    a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
+}
+
 static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, int sy, int sx, bool tf32 = false) {
     a.n = n;
     a.rows = rows;
@@ -685,22 +707,7 @@ static bool tc_configure(TcArgs& a, int n, int rows, int cols, int hy, int hx, i
     a.npass = 1 + ceil_div(std::max(0, O - (kTcRows - n)), kTcRows);
     // three operand stages where they fit in shared memory, else two
     for (a.nst = kTcMaxStages; a.nst >= 2; --a.nst) {
-        size_t o = 0;
-        auto take = [&](size_t bytes, size_t al) {
-            o = align_up(o, al);
-            size_t at = o;
-            o += bytes;
-            return (int)at;
-        };
-        a.off_stage = take((size_t)a.nst * (tf32 ? kTcStageBytesTf : kTcStageBytes), 1024);
-        a.z_bytes = (int)align_up((size_t)kTcKC * n * sizeof(cfloat), 16);
-        a.off_z = take(kTcZBuf * (size_t)a.z_bytes, 16);
-        a.off_pbits = take((size_t)kTcN * a.kwords * sizeof(uint32_t), 16);
-        a.off_soff = take((size_t)a.kpad * sizeof(int), 16);
-        a.off_runs = take((size_t)(a.kpad / kTcKC) * kTcRuns * sizeof(int2), 16);
-        a.off_rows = take((size_t)a.npass * kTcRows * sizeof(uint32_t), 16);
-        a.off_bar = take(128, 64);
-        a.smem_bytes = (int)align_up(o, 128) + 1024;  // + alignment slack
+        tc_carve(a, a.nst, n, a.kpad, a.npass, tf32);
         if (a.smem_bytes <= 227 * 1024) break;
     }
     return a.nst >= 2 && a.smem_bytes <= 227 * 1024;
@@ -725,14 +732,77 @@ static dpl_status launch_cov_tc(int n, int rows, int cols, int hy, int hx, int s
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int ntiles = a.tiles_r * a.tiles_c;
     const int grid = std::max(1, std::min(ntiles, sms));
+    TcBatch b{};
+    b.items[0] = a;
+    b.nitems = 1;
+    b.total = ntiles;
     if (tf32) {
-        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes));
-        k_cov_tc<true><<<grid, kTcThreads, a.smem_bytes, s>>>(a);
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          a.smem_bytes));
+        k_cov_tc<true, false><<<grid, kTcThreads, a.smem_bytes, s>>>(b, nullptr);
     } else {
-        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes));
-        k_cov_tc<false><<<grid, kTcThreads, a.smem_bytes, s>>>(a);
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          a.smem_bytes));
+        k_cov_tc<false, false><<<grid, kTcThreads, a.smem_bytes, s>>>(b, nullptr);
     }
     return check_launch("k_cov_tc");
+}
+
+// One work-queue launch of the covariance over the tiles of several stacks (items, each
+// configured by tc_configure with its pointers set, all of one operand type).  The items
+// go largest N first, and share one carve: the fewest stages any needs, the largest
+// sizes.  `counter` (device int) is zeroed on the stream first.
+static dpl_status launch_cov_tc_batch(std::vector<TcArgs> items, bool tf32, int* counter, cudaStream_t s) {
+    if (items.empty()) return DPL_OK;
+    if (items.size() > (size_t)kTcMaxItems) return fail(DPL_ERR_UNSUPPORTED, "batch: more than 16 stacks");
+    std::stable_sort(items.begin(), items.end(), [](const TcArgs& x, const TcArgs& y) { return x.n > y.n; });
+    int nst = kTcMaxStages, nmax = 0, kpad = 0, npass = 0;
+    for (const TcArgs& t : items) {
+        nst = std::min(nst, t.nst);
+        nmax = std::max(nmax, t.n);
+        kpad = std::max(kpad, t.kpad);
+        npass = std::max(npass, t.npass);
+    }
+    TcArgs carve{};
+    tc_carve(carve, nst, nmax, kpad, npass, tf32);
+    if (carve.smem_bytes > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "batch: covariance shared memory exceeds the SM limit");
+    TcBatch b{};
+    b.nitems = (int)items.size();
+    int total = 0;
+    for (int i = 0; i < b.nitems; ++i) {
+        TcArgs t = items[i];
+        t.nst = carve.nst;
+        t.off_stage = carve.off_stage;
+        t.z_bytes = carve.z_bytes;
+        t.off_z = carve.off_z;
+        t.off_pbits = carve.off_pbits;
+        t.off_soff = carve.off_soff;
+        t.off_runs = carve.off_runs;
+        t.off_rows = carve.off_rows;
+        t.off_bar = carve.off_bar;
+        t.smem_bytes = carve.smem_bytes;
+        t.status = items[0].status;
+        b.items[i] = t;
+        b.tile_start[i] = total;
+        total += t.tiles_r * t.tiles_c;
+    }
+    b.total = total;
+    if (total == 0) return DPL_OK;
+    int dev = 0, sms = 0;
+    DPL_CUDA_TRY(cudaGetDevice(&dev));
+    DPL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DPL_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+    const int grid = std::max(1, std::min(total, sms));
+    if (tf32) {
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          carve.smem_bytes));
+        k_cov_tc<true, true><<<grid, kTcThreads, carve.smem_bytes, s>>>(b, counter);
+    } else {
+        DPL_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          carve.smem_bytes));
+        k_cov_tc<false, true><<<grid, kTcThreads, carve.smem_bytes, s>>>(b, counter);
+    }
+    return check_launch("k_cov_tc (batch)");
 }
 
 static int norm_ref(int ref, int n) { return ref < 0 ? n + ref : ref; }
@@ -806,9 +876,23 @@ extern "C" size_t dpl_phase_link_workspace_size(const dpl_pl_params* p) {
                                nullptr);
 }
 
-// Enqueues the whole pipeline on `stream` without synchronising.
-static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
-                             void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
+// Per-call state between the pipeline's stages (pl_begin, then the covariance, then
+// pl_finish), so that a batch can run one covariance launch for several calls.
+struct PlState {
+    dpl_pl_params P;
+    const dpl_pl_inputs* in;
+    const dpl_pl_outputs* out;
+    PlWorkspace w;
+    PixArgs a;
+    int n, ref, out_rows, out_cols;
+    int64_t Pout;
+    bool tc_fits, tf32;
+    TcArgs tc;  // configured, pointers set, when tc_fits
+};
+
+// Validation, status words, k_prep and the per-pixel arguments of one call.
+static dpl_status pl_begin(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
+                           void* workspace, size_t workspace_bytes, cudaStream_t s, PlState& S) {
     if (!prm || !in || !out) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link: null argument");
     const dpl_pl_params& P = *prm;
     dpl_status st = validate_common(P.nslc, P.rows, P.cols, P.hy, P.hx, P.sy, P.sx);
@@ -826,12 +910,17 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
     if (P.nonconverged_mode < 0 || P.nonconverged_mode > 1)
         return fail(DPL_ERR_INVALID_ARGUMENT, "nonconverged_mode must be 0 or 1");
     if (workspace_bytes < dpl_phase_link_workspace_size(prm)) return fail(DPL_ERR_WORKSPACE, "workspace too small");
-    cudaStream_t s = (cudaStream_t)stream;
-    PlWorkspace w;
+    S.P = P;
+    S.in = in;
+    S.out = out;
+    S.n = n;
+    S.ref = ref;
+    PlWorkspace& w = S.w;
     pl_workspace_layout(P.nslc, P.rows, P.cols, P.sy, P.sx, P.cov_form, (char*)workspace, &w);
     const int64_t npix = P.rows * P.cols;
-    const int out_rows = (int)(P.rows / P.sy), out_cols = (int)(P.cols / P.sx);
-    const int64_t Pout = (int64_t)out_rows * out_cols;
+    S.out_rows = (int)(P.rows / P.sy);
+    S.out_cols = (int)(P.cols / P.sx);
+    S.Pout = (int64_t)S.out_rows * S.out_cols;
     DPL_CUDA_TRY(cudaMemsetAsync(w.status, 0, 64, s));
     DPL_CUDA_TRY(cudaMemsetAsync(w.valid_bits, 0, 64, s));
     {
@@ -843,85 +932,117 @@ static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, 
         st = check_launch("k_prep");
         if (st != DPL_OK) return st;
     }
-    if (Pout > 0) {
-        PixArgs a{};
-        fill_pix_layout(a, n, 2 * P.hx + 1);
-        a.rows = (int)P.rows;
-        a.cols = (int)P.cols;
-        a.hy = P.hy;
-        a.hx = P.hx;
-        a.sy = P.sy;
-        a.sx = P.sx;
-        a.out_rows = out_rows;
-        a.out_cols = out_cols;
-        a.npix = Pout;
-        a.zt = w.zt;
-        a.nb_u8 = in->neighbors;
-        set_solver_params(a, P.use_evd, P.beta, P.zero_correlation_threshold, ref, std::sqrt((double)P.hy * P.hx),
-                          P.first_real_slc_idx, P.compute_crlb);
-        a.baseline_lag = P.baseline_lag > 0 ? P.baseline_lag : 0;
-        a.slots = P.solver_slots;
-        a.lanes = P.solver_lanes;
-        a.nc_flag = P.nonconverged_mode == 0 ? out->nonconverged : nullptr;
-        a.eigh = P.nonconverged_mode == 0;
-        if (out->nonconverged) DPL_CUDA_TRY(cudaMemsetAsync(out->nonconverged, 0, (size_t)Pout, s));
-        a.vout = w.V;
-        a.eig = out->eigenvalues;
-        a.est = out->estimator;
-        a.crlb = w.CR;
-        a.tcoh = out->temp_coh;
-        a.closure = n > 2 ? out->closure_phases : nullptr;
-        a.counts = in->neighbors ? out->shp_counts : nullptr;
-        TcArgs tcfit{};
-        const bool tf32 = P.cov_form == 3;
-        const bool tc_fits = (P.cov_form == 0 || tf32) &&
-                             tc_configure(tcfit, n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, tf32);
-        if (P.cov_form == 2) {
-            // FP64 form: covariance and solver in double precision
-            st = timed(s, 0, [&] { return launch_pixel64(a, s); });
-        } else if (tc_fits) {
-            // chosen form: tensor-core covariance, then the solver on the planar matrices
-            st = timed(s, 0, [&] {
-                return launch_cov_tc(n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, w.zt, nullptr, 0,
-                                     in->neighbors, w.Cg, a.counts, w.status, s, tf32);
-            });
-            if (st != DPL_OK) return st;
-            a.Cplanar = w.Cg;
-            st = timed(s, 1, [&] {
-                return launch_pixel<kSolveOnly>(a, s, w.fb, P.nonconverged_mode == 0 ? w.nc : nullptr);
-            });
-        } else {
-            // plain form (or a window too large for the tensor-core tiles): SIMT covariance
-            // fused with the solver
-            st = timed(s, 0, [&] { return launch_pixel<kFused>(a, s, w.fb); });
-        }
-        if (st != DPL_OK) return st;
-
-        PostArgs q{};
-        q.n = n;
-        q.rows = (int)P.rows;
-        q.cols = (int)P.cols;
-        q.sy = P.sy;
-        q.sx = P.sx;
-        q.out_rows = out_rows;
-        q.out_cols = out_cols;
-        q.slc = reinterpret_cast<const cfloat*>(in->slc);
-        q.flags = w.flags;
-        q.mag = in->avg_mag ? in->avg_mag : w.avgmag;
-        q.V = w.V;
-        q.CR = w.CR;
-        q.use_max_ps = P.use_max_ps;
-        q.use_slc_amp = P.use_slc_amp;
-        q.ref_idx = ref;
-        q.cpx = reinterpret_cast<cfloat*>(out->cpx_phase);
-        q.tcoh = out->temp_coh;
-        q.crlb = out->crlb_std_dev;
-        q.status = w.status;
-        k_post<<<ceil_div(Pout, 256), 256, 0, s>>>(q);
-        st = check_launch("k_post");
-        if (st != DPL_OK) return st;
+    S.tc_fits = false;
+    S.tf32 = P.cov_form == 3;
+    if (S.Pout == 0) return DPL_OK;
+    PixArgs& a = S.a;
+    a = PixArgs{};
+    fill_pix_layout(a, n, 2 * P.hx + 1);
+    a.rows = (int)P.rows;
+    a.cols = (int)P.cols;
+    a.hy = P.hy;
+    a.hx = P.hx;
+    a.sy = P.sy;
+    a.sx = P.sx;
+    a.out_rows = S.out_rows;
+    a.out_cols = S.out_cols;
+    a.npix = S.Pout;
+    a.zt = w.zt;
+    a.nb_u8 = in->neighbors;
+    set_solver_params(a, P.use_evd, P.beta, P.zero_correlation_threshold, ref, std::sqrt((double)P.hy * P.hx),
+                      P.first_real_slc_idx, P.compute_crlb);
+    a.baseline_lag = P.baseline_lag > 0 ? P.baseline_lag : 0;
+    a.slots = P.solver_slots;
+    a.lanes = P.solver_lanes;
+    a.nc_flag = P.nonconverged_mode == 0 ? out->nonconverged : nullptr;
+    a.eigh = P.nonconverged_mode == 0;
+    if (out->nonconverged) DPL_CUDA_TRY(cudaMemsetAsync(out->nonconverged, 0, (size_t)S.Pout, s));
+    a.vout = w.V;
+    a.eig = out->eigenvalues;
+    a.est = out->estimator;
+    a.crlb = w.CR;
+    a.tcoh = out->temp_coh;
+    a.closure = n > 2 ? out->closure_phases : nullptr;
+    a.counts = in->neighbors ? out->shp_counts : nullptr;
+    S.tc = TcArgs{};
+    S.tc_fits = (P.cov_form == 0 || S.tf32) &&
+                tc_configure(S.tc, n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, S.tf32);
+    if (S.tc_fits) {
+        S.tc.zt = w.zt;
+        S.tc.bits = nullptr;
+        S.tc.wpr = 0;
+        S.tc.nb_u8 = in->neighbors;
+        S.tc.Cg = w.Cg;
+        S.tc.counts = a.counts;
+        S.tc.status = w.status;
     }
     return DPL_OK;
+}
+
+// The covariance (unless `cov_done`: a batch launched it), the solver and the post pass
+// of one call begun by pl_begin.
+static dpl_status pl_finish(PlState& S, cudaStream_t s, bool cov_done) {
+    if (S.Pout == 0) return DPL_OK;
+    const dpl_pl_params& P = S.P;
+    PlWorkspace& w = S.w;
+    PixArgs& a = S.a;
+    const int n = S.n;
+    dpl_status st;
+    if (P.cov_form == 2) {
+        // FP64 form: covariance and solver in double precision
+        st = timed(s, 0, [&] { return launch_pixel64(a, s); });
+    } else if (S.tc_fits) {
+        // chosen form: tensor-core covariance, then the solver on the planar matrices
+        if (!cov_done) {
+            st = timed(s, 0, [&] {
+                return launch_cov_tc(n, (int)P.rows, (int)P.cols, P.hy, P.hx, P.sy, P.sx, w.zt, nullptr, 0,
+                                     S.in->neighbors, w.Cg, a.counts, w.status, s, S.tf32);
+            });
+            if (st != DPL_OK) return st;
+        }
+        a.Cplanar = w.Cg;
+        st = timed(s, 1, [&] {
+            return launch_pixel<kSolveOnly>(a, s, w.fb, P.nonconverged_mode == 0 ? w.nc : nullptr);
+        });
+    } else {
+        // plain form (or a window too large for the tensor-core tiles): SIMT covariance
+        // fused with the solver
+        st = timed(s, 0, [&] { return launch_pixel<kFused>(a, s, w.fb); });
+    }
+    if (st != DPL_OK) return st;
+
+    PostArgs q{};
+    q.n = n;
+    q.rows = (int)P.rows;
+    q.cols = (int)P.cols;
+    q.sy = P.sy;
+    q.sx = P.sx;
+    q.out_rows = S.out_rows;
+    q.out_cols = S.out_cols;
+    q.slc = reinterpret_cast<const cfloat*>(S.in->slc);
+    q.flags = w.flags;
+    q.mag = S.in->avg_mag ? S.in->avg_mag : w.avgmag;
+    q.V = w.V;
+    q.CR = w.CR;
+    q.use_max_ps = P.use_max_ps;
+    q.use_slc_amp = P.use_slc_amp;
+    q.ref_idx = S.ref;
+    q.cpx = reinterpret_cast<cfloat*>(S.out->cpx_phase);
+    q.tcoh = S.out->temp_coh;
+    q.crlb = S.out->crlb_std_dev;
+    q.status = w.status;
+    k_post<<<ceil_div(S.Pout, 256), 256, 0, s>>>(q);
+    return check_launch("k_post");
+}
+
+// Enqueues the whole pipeline on `stream` without synchronising.
+static dpl_status pl_enqueue(const dpl_pl_params* prm, const dpl_pl_inputs* in, const dpl_pl_outputs* out,
+                             void* workspace, size_t workspace_bytes, dpl_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    PlState S;
+    dpl_status st = pl_begin(prm, in, out, workspace, workspace_bytes, s, S);
+    if (st != DPL_OK) return st;
+    return pl_finish(S, s, false);
 }
 
 // Maps the status words the pipeline left (status, then the 64 per-SLC "has a finite
@@ -996,6 +1117,71 @@ extern "C" dpl_status dpl_phase_link_status_words(int64_t nslc, const void* word
     if (!words) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link_status_words: null argument");
     const int* w = static_cast<const int*>(words);
     return pl_decode((int)nslc, w, reinterpret_cast<const unsigned int*>(w + 1));
+}
+
+// ---------------------------------------------------------------------------------
+// batches: several stacks (ministacks of uneven N) with one work-queue covariance launch
+// ---------------------------------------------------------------------------------
+static size_t batch_item_offset(const dpl_pl_params* prms, int i) {
+    size_t o = 256;  // two work-queue counters
+    for (int k = 0; k < i; ++k) o += align_up(dpl_phase_link_workspace_size(&prms[k]), 256);
+    return o;
+}
+
+extern "C" size_t dpl_phase_link_batch_workspace_size(const dpl_pl_params* prms, int count) {
+    if (!prms || count < 0) return 0;
+    return batch_item_offset(prms, count);
+}
+
+extern "C" dpl_status dpl_phase_link_batch(const dpl_pl_params* prms, const dpl_pl_inputs* ins,
+                                           const dpl_pl_outputs* outs, int count, void* workspace,
+                                           size_t workspace_bytes, dpl_stream_t stream) {
+    if (!prms || !ins || !outs || !workspace || count < 0)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link_batch: null argument");
+    if (count > kTcMaxItems) return fail(DPL_ERR_UNSUPPORTED, "dpl_phase_link_batch: at most 16 stacks per batch");
+    if (reinterpret_cast<uintptr_t>(workspace) & 255u)
+        return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link_batch: workspace must be 256-byte aligned");
+    if (workspace_bytes < dpl_phase_link_batch_workspace_size(prms, count))
+        return fail(DPL_ERR_WORKSPACE, "dpl_phase_link_batch: workspace too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    char* base = static_cast<char*>(workspace);
+    std::vector<PlState> S(count);
+    dpl_status st;
+    for (int i = 0; i < count; ++i) {
+        const size_t off = batch_item_offset(prms, i);
+        st = pl_begin(&prms[i], &ins[i], &outs[i], base + off, dpl_phase_link_workspace_size(&prms[i]), s, S[i]);
+        if (st != DPL_OK) return st;
+    }
+    // the tensor-core covariance of every stack that takes it: one work-queue launch per
+    // operand type
+    int* counters = reinterpret_cast<int*>(base);
+    for (int kind = 0; kind < 2; ++kind) {
+        std::vector<TcArgs> items;
+        for (int i = 0; i < count; ++i)
+            if (S[i].tc_fits && S[i].tf32 == (kind == 1)) items.push_back(S[i].tc);
+        if (items.empty()) continue;
+        st = timed(s, 0, [&] { return launch_cov_tc_batch(items, kind == 1, counters + kind, s); });
+        if (st != DPL_OK) return st;
+    }
+    for (int i = 0; i < count; ++i) {
+        st = pl_finish(S[i], s, S[i].tc_fits);
+        if (st != DPL_OK) return st;
+    }
+    return DPL_OK;
+}
+
+extern "C" dpl_status dpl_phase_link_batch_status(const dpl_pl_params* prms, int count, void* workspace,
+                                                  size_t workspace_bytes, dpl_stream_t stream) {
+    if (!prms || !workspace || count < 0) return fail(DPL_ERR_INVALID_ARGUMENT, "dpl_phase_link_batch_status: null argument");
+    if (workspace_bytes < dpl_phase_link_batch_workspace_size(prms, count))
+        return fail(DPL_ERR_WORKSPACE, "dpl_phase_link_batch_status: workspace too small");
+    for (int i = 0; i < count; ++i) {
+        const size_t off = batch_item_offset(prms, i);
+        dpl_status st = dpl_phase_link_status(&prms[i], static_cast<char*>(workspace) + off,
+                                              dpl_phase_link_workspace_size(&prms[i]), stream);
+        if (st != DPL_OK) return st;
+    }
+    return DPL_OK;
 }
 
 extern "C" size_t dpl_covariance_workspace_size(int64_t nslc, int64_t rows, int64_t cols) {

@@ -188,6 +188,22 @@ dpl_status dpl_phase_link_status_copy(const dpl_pl_params* params, void* workspa
                                       size_t workspace_bytes, void* words, dpl_stream_t stream);
 dpl_status dpl_phase_link_status_words(int64_t nslc, const void* words);
 
+/* Batches (not in the reference's API; its sequential workflow runs one ministack after
+ * another, workflows/sequential.py:105-147).  Enqueues `count` (<= 16) independent
+ * dpl_phase_link calls -- ministacks of uneven N, each with its own params, inputs and
+ * outputs -- on `stream` without synchronising.  The tensor-core covariance of all of
+ * them is one persistent launch whose CTAs take (stack, 16x16-pixel tile) items from a
+ * work queue, largest N first; the other stages run per stack.  The results are those
+ * of the separate calls.  workspace: dpl_phase_link_batch_workspace_size bytes, 256-byte
+ * aligned.  dpl_phase_link_batch_status synchronises `stream` and reports the first
+ * failing call's error, in order, as dpl_phase_link would. */
+size_t dpl_phase_link_batch_workspace_size(const dpl_pl_params* params, int count);
+dpl_status dpl_phase_link_batch(const dpl_pl_params* params, const dpl_pl_inputs* inputs,
+                                const dpl_pl_outputs* outputs, int count, void* workspace,
+                                size_t workspace_bytes, dpl_stream_t stream);
+dpl_status dpl_phase_link_batch_status(const dpl_pl_params* params, int count, void* workspace,
+                                       size_t workspace_bytes, dpl_stream_t stream);
+
 /* ---------------------------------------------------------------------------------
  * Stage entry points (used to check each stage against the oracle).
  * ------------------------------------------------------------------------------- */

@@ -100,3 +100,40 @@ def test_solver_instances_agree(n):
         assert float((out.temp_coh - ref.temp_coh)[good].abs().max()) < 1e-5
         fin = torch.isfinite(ref.crlb_std_dev)
         assert torch.equal(fin, torch.isfinite(out.crlb_std_dev))
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_persistent_batch_n8_n45(graph):
+    """The persistent path (one work-queue covariance launch for every stack): N = 8 and
+    45 with the bf16 and the tf32 covariance, bit-identical to the per-stack path, and
+    against the oracle."""
+    from oracle import phase_link as O
+
+    hw = (5, 5)  # 121 samples: full-rank coherence at N = 45
+    stacks = [torch.from_numpy(make_stack(StackConfig(nslc=n, rows=44, cols=52, seed=960 + k, ps_frac=0.02,
+                                                      outlier_frac=0.3))).cuda() for k, n in enumerate((8, 45, 12, 45))]
+    forms = {8: "tensor", 45: "tensor", 12: "tf32"}
+    per = PhaseLinkBatch(stacks, hw, forms=forms, graph=False, persistent=False).run()
+    outs = PhaseLinkBatch(stacks, hw, forms=forms, graph=graph, persistent=True).run()
+    for z, a, b in zip(stacks, outs, per):
+        for x, y in zip(a, b):
+            assert torch.equal(torch.nan_to_num(x.float() if not x.is_complex() else torch.view_as_real(x), 7.0),
+                               torch.nan_to_num(y.float() if not y.is_complex() else torch.view_as_real(y), 7.0))
+    for k in (0, 1):  # N = 8 and 45 against the oracle
+        z = stacks[k].cpu().numpy()
+        n = z.shape[0]
+        mean, disp, ps = O.calc_ps_block(np.abs(z), 0.25, n)
+        nb = O.estimate_neighbors_glrt(mean, (disp * mean) ** 2, hw, (1, 1), n, 0.001)
+        ref = O.run_phase_linking(z, hw, ps_mask=ps.copy(), neighbor_arrays=nb, avg_mag=mean, dtype=np.float64,
+                                  eigh_fallback=True)
+        out = outs[k]
+        # well-conditioned pixels: at least twice as many SHP samples as SLCs (near N
+        # samples the sample coherence is close to singular and float32 rounding of C
+        # moves the eigenvector by more than 1e-3 rad)
+        good = (ref.temp_coh > 0.3) & np.all(np.isfinite(ref.cpx_phase), axis=0) & \
+            (out.estimator.cpu().numpy() == ref.estimator) & (ref.shp_counts >= 2 * n)
+        assert good.sum() > 0
+        err = phase_err(out.cpx_phase.cpu().numpy()[:, good], ref.cpx_phase[:, good].astype(np.complex64))
+        print(f"persistent batch N={n}: max phase error {err.max():.2e} rad vs the float64 oracle on "
+              f"{int(good.sum())} pixels")
+        assert err.max() < 1e-3
