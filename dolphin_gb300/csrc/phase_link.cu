@@ -266,9 +266,9 @@ __global__ void __launch_bounds__(32) k_eigh(PixArgs a, EighLayout L) {
     const int lane = threadIdx.x;
     cfloat* C = reinterpret_cast<cfloat*>(eigh_smem + L.off_C);
     cfloat* A = reinterpret_cast<cfloat*>(eigh_smem + L.off_A);
-    cfloat* V = reinterpret_cast<cfloat*>(eigh_smem + L.off_V);
     double* G = reinterpret_cast<double*>(eigh_smem + L.off_G);
-    cfloat* w = reinterpret_cast<cfloat*>(eigh_smem + L.off_w);
+    const EighVec V = eigh_vectors(eigh_smem, L);
+    cfloat* w = V.w;
     const int n = a.n, ld = L.ld, lag = a.baseline_lag;
     const int count = *a.nc_count;
     for (int idx = blockIdx.x; idx < count; idx += gridDim.x) {
@@ -309,54 +309,35 @@ __global__ void __launch_bounds__(32) k_eigh(PixArgs a, EighLayout L) {
         const bool evd = a.est[p] == 0;  // the estimator the solver chose
         bool ok = true;
         if (!evd) {
-            // |Gamma| + 1e-6 I inverted in double; A = |Gamma|^{-1} o C
+            // |Gamma| + 1e-6 I inverted in double; A = |Gamma|^{-1} o C (lower triangles)
             for (int i = 0; i < n; ++i)
-                for (int j = lane; j < n; j += 32)
+                for (int j = lane; j <= i; j += 32)
                     G[i * n + j] = (double)s_gamma(a, C[i * ld + j], i == j) + (i == j ? 1e-6 : 0.0);
-            ok = e_inverse_spd(G, n, lane);
+            ok = e_inverse_spd(G, G + n * n, n, lane);
             if (ok)
                 for (int i = 0; i < n; ++i)
-                    for (int j = lane; j < n; j += 32) A[i * ld + j] = cscale(C[i * ld + j], (float)G[i * n + j]);
+                    for (int j = lane; j <= i; j += 32) A[i * ld + j] = cscale(C[i * ld + j], (float)G[i * n + j]);
         } else {
             for (int i = 0; i < n; ++i)
-                for (int j = lane; j < n; j += 32) {
+                for (int j = lane; j <= i; j += 32) {
                     const cfloat c = C[i * ld + j];
                     A[i * ld + j] = cscale(c, sqrtf(c.re * c.re + c.im * c.im));
                 }
         }
         __syncwarp();
         if (ok) {
-            e_jacobi(A, V, n, ld, lane);
             // EMI: the eigenvalue nearest the shift 0.99; EVD: the largest in magnitude
-            float best = INFINITY;
-            int bi = n;
-            for (int i = lane; i < n; i += 32) {
-                const float lam = A[i * ld + i].re;
-                const float score = evd ? -fabsf(lam) : fabsf(lam - 0.99f);
-                if (score < best) {
-                    best = score;
-                    bi = i;
-                }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob < best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
-                }
-            }
-            if (bi < n) {
-                const float lambda = A[bi * ld + bi].re;
+            cfloat* x = V.pw;
+            const float lambda = e_eigpair(A, n, ld, evd, V, x, lane);
+            {
                 float s2 = 0.f;
-                for (int i = lane; i < n; i += 32) s2 += cabs2(V[i * ld + bi]);
+                for (int i = lane; i < n; i += 32) s2 += cabs2(x[i]);
                 s2 = warp_sum(s2);
                 const float scale = (evd ? 1.f : sqrtf((float)n)) / sqrtf(s2);
-                const cfloat rot = cconj(fphasor(V[a.ref_idx * ld + bi]));
+                const cfloat rot = cconj(fphasor(x[a.ref_idx]));
                 __syncwarp();
                 for (int i = lane; i < n; i += 32) {
-                    const cfloat v = cmul(cscale(V[i * ld + bi], scale), rot);
+                    const cfloat v = cmul(cscale(x[i], scale), rot);
                     a.vout[p * n + i] = v;
                     w[i] = fphasor(v);
                 }
@@ -622,12 +603,15 @@ static dpl_status launch_pixel64(const PixArgs& a, cudaStream_t s) {
 // grid of up to 8 per SM (the list length is known only on the device).
 static dpl_status launch_eigh(const PixArgs& a, cudaStream_t s) {
     const EighLayout L = make_eigh_layout(a.n);
-    if (L.bytes > 227 * 1024) return fail(DPL_ERR_UNSUPPORTED, "eigensolver: shared memory exceeds the SM limit");
-    int dev = 0, sms = 0;
+    if (a.n > kEighMaxN || L.bytes > 227 * 1024)
+        return fail(DPL_ERR_UNSUPPORTED, "eigensolver: N above 64 or shared memory above the SM limit");
+    int dev = 0, sms = 0, per_sm = 0;
     DPL_CUDA_TRY(cudaGetDevice(&dev));
     DPL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     DPL_CUDA_TRY(cudaFuncSetAttribute(k_eigh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes));
-    k_eigh<<<(unsigned)std::max(1, sms * 8), 32, L.bytes, s>>>(a, L);
+    DPL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh, 32, L.bytes));
+    // one resident wave: each warp strides over the listed pixels
+    k_eigh<<<(unsigned)std::max(1, sms * std::max(1, per_sm)), 32, L.bytes, s>>>(a, L);
     return check_launch("k_eigh");
 }
 

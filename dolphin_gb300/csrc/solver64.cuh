@@ -317,14 +317,18 @@ __device__ bool iterate64(cdbl (&v)[NB], Op&& op) {
     return !(diff > 1e-5);  // a NaN difference ends the loop too, as in the reference
 }
 
-// The dense eigensolver of the non-convergence fallback (eigh.cuh) in double: cyclic
-// Jacobi on the Hermitian A (n x n, both triangles), eigenvectors in the columns of V,
-// eigenvalues on the diagonal of A.
+// The dense eigensolver of the non-convergence fallback in double (the FP64 form is a
+// reference form, so the whole spectrum is computed): cyclic Jacobi for Hermitian
+// matrices (Golub & Van Loan, Matrix Computations, section 8.5; each rotation removes
+// the pivot's phase with a diagonal unitary, then applies the real rotation) on A (n x n,
+// both triangles), eigenvectors in the columns of V, eigenvalues on the diagonal of A.
+constexpr int kJacobiMaxSweeps = 30;
+
 __device__ inline void e_jacobi64(cdbl* A, cdbl* V, int n, int lane) {
     for (int i = 0; i < n; ++i)
         for (int j = lane; j < n; j += 32) V[i * n + j] = dmk(i == j ? 1.0 : 0.0, 0.0);
     __syncwarp();
-    for (int sweep = 0; sweep < kEighMaxSweeps; ++sweep) {
+    for (int sweep = 0; sweep < kJacobiMaxSweeps; ++sweep) {
         double off = 0.0, tot = 0.0;
         for (int i = 0; i < n; ++i)
             for (int j = lane; j < n; j += 32) {
