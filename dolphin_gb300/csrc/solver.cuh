@@ -45,13 +45,13 @@ struct SolveMats {
     int* piv;    // 128 ints (LU pass)
 };
 
-// unit phasor exp(i angle(c)) via rsqrt; angle(+0) = 0, angle(-0 + 0j) = pi
+// unit phasor exp(i angle(c)) via rsqrt, without branches; angle(+0) = 0,
+// angle(-0 + 0j) = pi, NaN stays NaN
 __device__ __forceinline__ cfloat fphasor(cfloat c) {
     const float m2 = c.re * c.re + c.im * c.im;
-    if (m2 == 0.f) return cmake(signbit(c.re) ? -1.f : 1.f, 0.f);
-    if (!(m2 <= INFINITY)) return cmake(nanf(""), nanf(""));
     const float r = rsqrtf(m2);
-    return cmake(c.re * r, c.im * r);
+    const bool z = m2 == 0.f;
+    return cmake(z ? copysignf(1.f, c.re) : c.re * r, z ? 0.f : c.im * r);
 }
 
 // In-place inverse of a symmetric positive definite n x n matrix by Gauss-Jordan
@@ -265,7 +265,12 @@ __device__ void s_lu_solve(const cfloat* A, int n, const int* src, cfloat (&x)[N
 }
 
 __device__ __forceinline__ float s_gamma(const PixArgs& a, cfloat c, bool diag) {
-    float g = sqrtf(c.re * c.re + c.im * c.im);
+    // |c|: the correctly rounded square root where the zero-correlation threshold
+    // compares it, the approximate one (relative error below 2^-22) otherwise
+    const float m2 = c.re * c.re + c.im * c.im;
+    float g;
+    if (a.zct > 0.f) g = sqrtf(m2);
+    else asm("sqrt.approx.f32 %0, %1;" : "=f"(g) : "f"(m2));
     if (a.beta_on) g = fadd(fmul(a.one_minus_beta, g), diag ? a.beta : 0.f);
     return g < a.zct ? 0.f : g;
 }

@@ -26,7 +26,7 @@ namespace dpl {
 
 // Shared memory per pixel group: full Hermitian C (n x ld, ld odd: a thread-per-row
 // access of one column is conflict-free), |Gamma| / |Gamma|^{-1} (n x ld floats), a
-// 64-entry broadcast buffer, a 64-entry vector buffer and reduction slots.
+// 128-entry broadcast buffer, a 64-entry vector buffer and reduction slots.
 struct RegLayout {
     int ld;
     size_t off_C, off_G, off_b, off_w, off_x, bytes;
@@ -43,7 +43,7 @@ inline RegLayout make_reg_layout(int n) {
     };
     L.off_C = take((size_t)n * L.ld * sizeof(cfloat));
     L.off_G = take((size_t)n * L.ld * sizeof(float));
-    L.off_b = take(64 * sizeof(cfloat));
+    L.off_b = take(128 * sizeof(cfloat));  // the sweeps' two broadcast halves
     L.off_w = take(64 * sizeof(cfloat));
     L.off_x = take(16 * sizeof(float));
     L.bytes = align_up(o, 128);
@@ -107,28 +107,35 @@ struct Grp {
     }
 };
 
-// Broadcast position of row `row`'s pivot-column entry before step k: (row - k) mod K
-// (slot s of every row then reads position s).  K is even; row, k < K.
-template <int K>
-__device__ __forceinline__ int slot_pos(int row, int k) {
-    if ((K & (K - 1)) == 0) return (row - k) & (K - 1);
-    const int d = row - k;
-    return d < 0 ? d + K : d;
+// 1/p to about an ulp: the approximate reciprocal refined by one Newton step.
+__device__ __forceinline__ float frcp_nr(float p) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(p));
+    return fmaf(r, fmaf(-p, r, 1.f), r);
 }
+
+// The sweeps broadcast the pivot column through `buf`, two halves used alternately so
+// that one barrier per step suffices: step k writes half k & 1, whose readers (step
+// k - 2) all passed step k - 1's barrier before this thread did.  Row `gl` writes its
+// pivot-column entry at position (gl - k) mod K, so slot s of every row reads position s.
 
 // Real symmetric sweep over indices 0..n-1 of the matrix whose row `gl` is g; on
 // success g holds row `gl` of -A^{-1}.  Returns false (uniformly) if any pivot was
 // <= 0 (the remaining steps then run on meaningless values, without branching).
+// buf: 2 * ((K + 3) & ~3) floats.
 template <int K, int G>
 __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, const Grp<G>& gr) {
-    bool bad = false;  // uniform: every thread reads the same pivot
+    constexpr int KB = (K + 3) & ~3;  // half stride: 16-byte aligned
+    bool bad = false;                 // uniform: every thread reads the same pivot
+    int pos = gr.gl;
+    gr.sync();  // earlier users of buf are done with it
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
-        gr.sync();
-        if (gr.gl < K) buf[slot_pos<K>(gr.gl, k)] = g[0];  // A[row][k] (= A[k][row])
+        float* bk = buf + (k & 1) * KB;
+        if (gr.gl < K) bk[pos] = g[0];  // A[row][k] (= A[k][row])
         gr.sync();
         float r[K];
-        const float4* b4 = reinterpret_cast<const float4*>(buf);
+        const float4* b4 = reinterpret_cast<const float4*>(bk);
 #pragma unroll
         for (int q = 0; q < K / 4; ++q) {
             const float4 t = b4[q];
@@ -138,13 +145,13 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, const 
             r[4 * q + 3] = t.w;
         }
         if (K % 4) {  // K = 4m + 2: the last two slots
-            const float2 t = reinterpret_cast<const float2*>(buf)[K / 2 - 1];
+            const float2 t = reinterpret_cast<const float2*>(bk)[K / 2 - 1];
             r[K - 2] = t.x;
             r[K - 1] = t.y;
         }
         const float p = r[0];
         bad |= !(p > 0.f);
-        const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
+        const float ip = frcp_nr(p);
         const bool me = gr.gl == k;
         // rows i != k: a_ij - (a_ik / p) a_kj; row k: a_kj / p, written as
         // a_kj - (1 - 1/p) a_kj so that every thread runs the same FMA
@@ -153,6 +160,7 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, const 
 #pragma unroll
         for (int s = 0; s < K - 1; ++s) g[s] = fmaf(-t, r[s + 1], g[s + 1]);
         g[K - 1] = last;
+        pos = pos == 0 ? K - 1 : pos - 1;
     }
 #pragma unroll 1
     for (int k = n; k < K; ++k) {  // finish the rotation: slot s holds column s again
@@ -166,21 +174,24 @@ __device__ __forceinline__ bool r_sweep(float (&g)[K], int n, float* buf, const 
 }
 
 // Hermitian sweep: on success a holds row `gl` of -A^{-1}.  False if a pivot was <= 0.
+// buf: 2 * K complex.
 template <int K, int G>
 __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, const Grp<G>& gr) {
     bool bad = false;  // uniform: every thread reads the same pivot
+    int pos = gr.gl;
+    gr.sync();
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
+        cfloat* bk = buf + (k & 1) * K;  // K even: 16-byte aligned halves
+        if (gr.gl < K) bk[pos] = a[0];   // A[row][k] = conj(A[k][row])
         gr.sync();
-        if (gr.gl < K) buf[slot_pos<K>(gr.gl, k)] = a[0];  // A[row][k] = conj(A[k][row])
-        gr.sync();
-        const float p = buf[0].re;
+        const float p = bk[0].re;
         bad |= !(p > 0.f);
-        const float ip = __frcp_rn(p);  // = 1.f / p, correctly rounded
+        const float ip = frcp_nr(p);
         const bool me = gr.gl == k;
         const cfloat t = me ? cmake(1.f - ip, 0.f) : cscale(a[0], ip);
         const cfloat last = me ? cmake(-ip, 0.f) : cscale(a[0], ip);
-        const float4* b4 = reinterpret_cast<const float4*>(buf);
+        const float4* b4 = reinterpret_cast<const float4*>(bk);
 #pragma unroll
         for (int q = 0; q < K / 2; ++q) {
             const float4 b = b4[q];
@@ -189,6 +200,7 @@ __device__ __forceinline__ bool r_sweep_c(cfloat (&a)[K], int n, cfloat* buf, co
             a[2 * q] = cfms_conj(a[2 * q + 1], t, cmake(b.z, b.w));
         }
         a[K - 1] = last;
+        pos = pos == 0 ? K - 1 : pos - 1;
     }
 #pragma unroll 1
     for (int k = n; k < K; ++k) {
@@ -222,6 +234,8 @@ __device__ __forceinline__ cfloat r_matvec(const cfloat (&h)[K], cfloat x, cfloa
 template <int G>
 __device__ __forceinline__ void r_prefetch(float* dst, const float* src, int count, const Grp<G>& gr) {
     gr.sync();
+    // 4-byte pieces: 16-byte copies measured slower here (the solve is issue-bound and
+    // the copy has the whole temporal-coherence pass to land)
     for (int e = gr.gl; e < count; e += G)
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + e)),
                      "l"(src + e)
@@ -237,7 +251,7 @@ __device__ __forceinline__ float r_iterate(cfloat& v, const Grp<G>& gr, int& ste
     float diff = 1.f;
     for (int it = 1; diff > 1e-5f && it < 50; ++it) {
         cfloat x = op(v);
-        const float inv = 1.f / sqrtf(gr.sum(cabs2(x)));
+        const float inv = rsqrtf(gr.sum(cabs2(x)));
         x = cscale(x, inv);
         diff = sqrtf(gr.sum(cabs2(csub(x, v))));
         v = x;
@@ -269,16 +283,18 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     bool crlb_ok = false;
     float dg = 0.f;
     if (!(a.use_evd && !a.compute_crlb)) {
-        // |Gamma| row by a compact loop into shared memory, then into the register slots
-        if (row)
-            for (int j = 0; j < n; ++j) Gi[j] = s_gamma(a, Ci[j], j == me);
+        // |Gamma| + 1e-6 I row by a compact loop into shared memory, then into the
+        // register slots; the diagonal of |Gamma| itself is kept in gdiag
+        const int nr = row ? n : 0;  // this row's live columns
+        float gdiag = 0.f;
+        for (int j = 0; j < nr; ++j) {
+            const float gm = s_gamma(a, Ci[j], j == me);
+            if (j == me) gdiag = gm;
+            Gi[j] = j == me ? fadd(gm, 1e-6f) : gm;
+        }
         float g[K];
 #pragma unroll
-        for (int j = 0; j < K; ++j) {
-            float x = 0.f;
-            if (row && j < n) x = j == me ? fadd(Gi[j], 1e-6f) : Gi[j];
-            g[j] = x;
-        }
+        for (int j = 0; j < K; ++j) g[j] = j < nr ? Gi[j] : 0.f;
 #pragma unroll 1
         for (int round = 0; round < 2; ++round) {
             const bool ok = r_sweep<K, G>(g, n, reinterpret_cast<float*>(cb), gr);
@@ -297,17 +313,16 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
                 inv_nan = gr.any(bad);
             }
             // keep |Gamma|^{-1} and build the FIM in place of it
+            const bool refrow = me == ref;
 #pragma unroll
             for (int j = 0; j < K; ++j) {
                 const float ginv = -g[j];
                 float x = 0.f;
-                if (row && j < n) {
-                    if (me == ref || j == ref) {
-                        x = j == me ? 1.f : 0.f;
-                    } else {
-                        x = fmul(a.crlb_factor, fsub(fmul(Gi[j], ginv), j == me ? 1.f : 0.f));
-                        if (j == me) x = fadd(x, 1e-6f);
-                    }
+                if (j < nr) {
+                    const bool dj = j == me;
+                    x = fmul(a.crlb_factor, fsub(fmul(dj ? gdiag : Gi[j], ginv), dj ? 1.f : 0.f));
+                    if (dj) x = fadd(x, 1e-6f);
+                    if (refrow || j == ref) x = dj ? 1.f : 0.f;
                     Gi[j] = ginv;
                 }
                 g[j] = x;
@@ -406,6 +421,7 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     gr.sync();
     float sre = 0.f, sim = 0.f, cnt = 0.f;
     const int npairs = n * (n - 1) / 2;
+#pragma unroll 2
     for (int e = me; e < npairs; e += G) {
         const uint32_t rc = ptab[e];
         const int r = rc & 0xffff, c = rc >> 16;
@@ -490,6 +506,7 @@ __global__ void __launch_bounds__(256, G == 64 ? 1 : 2) k_solve_reg(PixArgs a, R
                 Cf[me * ld + me] = cmake(f < 1e6f ? src[me] * f : 0.f, 0.f);
             }
             const int npairs = n * (n - 1) / 2;
+#pragma unroll 2
             for (int e = me; e < npairs; e += G) {
                 const uint32_t rc = ptab[e];
                 const int r = rc & 0xffff, c = rc >> 16;
