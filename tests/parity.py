@@ -135,7 +135,16 @@ def compare_workflow(out, ref, tc_min=0.3, phase_tol=1e-3, tc_tol=1e-4, sim_tol=
     # layers), as for a single phase-linking call
     n_layers = ref["clos"].shape[-1] + 2
     posed = good & (np.asarray(out["est"]) == np.asarray(ref["est"])) & (np.asarray(ref["counts"]) >= n_layers)
-    np.testing.assert_allclose(out["eig"][posed], ref["eig"][posed], rtol=eig_rtol, atol=1e-4)
+    e_out, e32 = np.asarray(out["eig"])[posed], np.asarray(ref["eig"])[posed]
+    off = ~np.isclose(e_out, e32, rtol=eig_rtol, atol=1e-4)
+    if off.any() and ref64 is not None:
+        # where the float32 runs disagree the float64 run decides (an ill-conditioned
+        # |Gamma| amplifies float32 rounding in the eigenvalue)
+        e64 = np.asarray(ref64["eig"])[posed]
+        print(f"{label}: {int(off.sum())} eigenvalues off the float32 run: got {e_out[off]}, float32 {e32[off]}, "
+              f"float64 {e64[off]}")
+        off &= ~np.isclose(e_out, e64, rtol=eig_rtol, atol=1e-4)
+    assert not off.any(), (e_out[off], e32[off])
     np.testing.assert_allclose(out["crlb"][:, posed], ref["crlb"][:, posed], rtol=crlb_rtol, atol=1e-5)
     # compressed SLC: mean amplitude and the phase of the projection on the linked phases
     np.testing.assert_array_equal(np.isnan(out["comp"]), np.isnan(ref["comp"]))
