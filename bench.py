@@ -42,9 +42,10 @@ METRIC = "phase-linked pixels/sec (N=30, EMI) chosen vs plain GPU form at <=1e-3
 # 3,772,850,944); the planar coherence output (N^2 floats per pixel) is most of it
 COV_TC_TRAFFIC = 612_392_704 + 3_772_850_944
 # DRAM bytes (read + write) of one k_solve_reg launch on a 1034x1046-pixel block, scaled
-# from an ncu capture of the 778x790 block by the pixel count (the planar coherence read,
-# N^2 floats per pixel, is most of it); None until captured
-SOLVE_TRAFFIC = None
+# by the pixel count from an ncu capture of the 778x790 block (614,620 pixels:
+# dram__bytes.sum.per_second 239.94 GB/s over 10.005 ms = 2.4006 GB, 3,905.8 B per pixel;
+# the planar coherence read, N^2 floats per pixel, is most of it)
+SOLVE_TRAFFIC = round(2.4006e9 / 614_620 * 1034 * 1046)
 UNIT = "pixels/s"
 
 
