@@ -124,15 +124,16 @@ typedef struct dpl_pl_params {
                                       form); 2: covariance and solver in FP64 (the double-precision reference
                                       form); 3: tensor-core covariance with tf32 operands (one product) */
     /* Not in the reference (zero = default).  Register-solver instance: row slots K (even,
-     * >= nslc; 0 = nslc rounded up to even) and threads per pixel (8, 16 or 32 for K <= 32;
-     * 0 = the smallest power of two >= K); a tuner's choices: the same algorithm, group
-     * reductions may round differently. */
+     * >= nslc; 0 = nslc rounded up to even) and threads per pixel (8, 16 or 32 for K <= 32,
+     * at least K; 0 = the smallest power of two >= max(K, 8); K > 32 always uses two warps);
+     * a tuner's choices: the same algorithm, group reductions may round differently. */
     int solver_slots;
     int solver_lanes;
     /* Not in the reference.  Pixels whose eigen-iteration misses the stopping rule within
      * 49 steps (the reference returns that last iterate, _eigenvalues.py:194-202):
      * 0 (default) -- solved again by a dense Hermitian eigensolver (|Gamma| inverted in
-     * double precision, cyclic Jacobi) and flagged in outputs->nonconverged; 1 -- keep
+     * double precision; Householder tridiagonalisation, Sturm multisection and inverse
+     * iteration for the wanted eigenpair) and flagged in outputs->nonconverged; 1 -- keep
      * the last iterate, as the reference does.  Applies to the tensor-core form (the
      * forms that store the coherence). */
     int nonconverged_mode;
