@@ -283,15 +283,23 @@ __device__ void solve_pixel_reg(const PixArgs& a, int64_t p, const cfloat* Cf, f
     bool crlb_ok = false;
     float dg = 0.f;
     if (!(a.use_evd && !a.compute_crlb)) {
-        // |Gamma| + 1e-6 I row by a compact loop into shared memory, then into the
-        // register slots; the diagonal of |Gamma| itself is kept in gdiag
+        // |Gamma| + 1e-6 I into shared memory by lower pairs (every thread busy), the
+        // diagonal of |Gamma| itself kept in gdiag, then into the register slots
         const int nr = row ? n : 0;  // this row's live columns
-        float gdiag = 0.f;
-        for (int j = 0; j < nr; ++j) {
-            const float gm = s_gamma(a, Ci[j], j == me);
-            if (j == me) gdiag = gm;
-            Gi[j] = j == me ? fadd(gm, 1e-6f) : gm;
+        const int npairs = n * (n - 1) / 2;
+        for (int e = me; e < npairs; e += G) {
+            const uint32_t rc = ptab[e];
+            const int r = rc & 0xffff, c = rc >> 16;
+            const float gm = s_gamma(a, Cf[r * ld + c], false);
+            Gs[r * ld + c] = gm;
+            Gs[c * ld + r] = gm;
         }
+        float gdiag = 0.f;
+        if (row) {
+            gdiag = s_gamma(a, Ci[me], true);
+            Gi[me] = fadd(gdiag, 1e-6f);
+        }
+        gr.sync();
         float g[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) g[j] = j < nr ? Gi[j] : 0.f;
