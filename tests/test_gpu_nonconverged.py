@@ -73,3 +73,25 @@ def test_eigh_fallback_off_is_the_reference_iterate(case):
     err = phase_err(out.cpx_phase[:, good & ~flip], ref.cpx_phase[:, good & ~flip]).max()
     print(f"last iterates vs the float32 oracle: max phase error {err:.2e} rad")
     assert err <= 5e-3
+
+
+def test_evd_nonconverged_pixels_against_float64(case):
+    # EVD: power iteration on C o |C| converges at the ratio of its two largest
+    # eigenvalues, so on this stack many pixels miss the rule; the dense eigensolver's
+    # target is then the eigenvalue of largest magnitude
+    z, nb, _ref64, _nc64 = case
+    flags = np.zeros(z.shape[1:], np.uint8)
+    out = dp.run_phase_linking(z, HW, neighbor_arrays=nb, use_evd=True, nonconverged=flags)
+    diag = {}
+    ref64 = O.run_phase_linking(z, HW, neighbor_arrays=nb, use_evd=True, dtype=np.float64, eigh_fallback=True,
+                                diagnostics=diag)
+    f = flags.astype(bool)
+    assert f.sum() > 0
+    good = (ref64.temp_coh > 0.3) & np.all(np.isfinite(ref64.cpx_phase), axis=0)
+    err = phase_err(out.cpx_phase[:, good], ref64.cpx_phase[:, good].astype(np.complex64)).max(0)
+    ef = err[f[good]]
+    print(f"EVD: {int(f.sum())} flagged on the GPU, {int(diag['nonconverged'].sum())} in float64; phase error vs "
+          f"float64 on the flagged coherent ones max {ef.max() if ef.size else 0:.2e} rad, on all "
+          f"{int(good.sum())} coherent pixels max {err.max():.2e} rad")
+    assert ef.size and ef.max() <= 1e-3
+    assert np.abs(out.temp_coh[good] - ref64.temp_coh[good]).max() <= 1e-4
