@@ -25,12 +25,12 @@ namespace dpl {
 
 constexpr int kEighMaxN = 64;
 
-// Shared-memory layout of one warp's pixel: C and A (n x ld complex, ld odd), the
-// double |Gamma| work matrix (n x n, then an n-long work column) and the per-pixel
-// vectors.
+// Shared-memory layout of one warp's pixel: C and A (n x ld complex, ld odd; the double
+// |Gamma| work matrix shares A's storage, element for element, until A is formed), two
+// n-long double work columns and the per-pixel vectors.
 struct EighLayout {
     int ld;
-    size_t off_C, off_A, off_G, off_w, off_vec, bytes;
+    size_t off_C, off_A, off_col, off_w, off_vec, bytes;
 };
 
 // the float vectors of one pixel, each kEighMaxN long
@@ -58,7 +58,7 @@ inline EighLayout make_eigh_layout(int n) {
     };
     L.off_C = take((size_t)n * L.ld * sizeof(cfloat));
     L.off_A = take((size_t)n * L.ld * sizeof(cfloat));
-    L.off_G = take(((size_t)n * n + kEighMaxN) * sizeof(double));  // G, then a work column
+    L.off_col = take(2 * kEighMaxN * sizeof(double));
     L.off_w = take(kEighMaxN * sizeof(cfloat));
     L.off_vec = take(kEighMaxN * (2 * sizeof(cfloat) + 7 * sizeof(float)));
     L.bytes = align_up(o, 128);
@@ -91,35 +91,40 @@ __device__ __forceinline__ void tri_step(int& i, int& j, int step) {
     }
 }
 
-// In-place inverse of the symmetric positive definite n x n double matrix G (lower
-// triangle read and written) by the sweep operator: sweeping pivot k maps
+// In-place inverse of the symmetric positive definite n x n double matrix G (row stride
+// ld; lower triangle read and written) by the sweep operator: sweeping pivot k maps
 // g_kk -> -1/g_kk, g_ik -> g_ik/g_kk, g_ij -> g_ij - g_ik g_kj / g_kk; after all n pivots
-// G holds -G^{-1}, negated at the end.  col is an n-long double work vector.  False on
-// a non-positive pivot (the matrix is not positive definite).
-__device__ inline bool e_inverse_spd(double* G, double* col, int n, int lane) {
+// G holds -G^{-1}, negated at the end.  col and cinv are n-long double work vectors
+// (column k, and column k / g_kk, so that each update is one fused multiply-add on the
+// narrow FP64 pipe).  False on a non-positive pivot (not positive definite).
+__device__ inline bool e_inverse_spd(double* G, int ld, double* col, double* cinv, int n, int lane) {
     for (int k = 0; k < n; ++k) {
         __syncwarp();
-        const double piv = G[k * n + k];
+        const double piv = G[k * ld + k];
         if (!(piv > 0.0)) return false;
         const double inv = 1.0 / piv;
-        for (int i = lane; i < n; i += 32) col[i] = i >= k ? G[i * n + k] : G[k * n + i];
+        for (int i = lane; i < n; i += 32) {
+            const double c = i >= k ? G[i * ld + k] : G[k * ld + i];
+            col[i] = c;
+            cinv[i] = c * inv;
+        }
         __syncwarp();
         int i = 0, j = lane;
         tri_step(i, j, 0);
         for (; i < n; tri_step(i, j, 32))
-            if (i != k && j != k) G[i * n + j] -= col[i] * col[j] * inv;
+            if (i != k && j != k) G[i * ld + j] = fma(-col[i], cinv[j], G[i * ld + j]);
         __syncwarp();
         for (int t = lane; t < n; t += 32) {
             if (t == k) continue;
-            if (t > k) G[t * n + k] = col[t] * inv;
-            else G[k * n + t] = col[t] * inv;
+            if (t > k) G[t * ld + k] = cinv[t];
+            else G[k * ld + t] = cinv[t];
         }
-        if (lane == 0) G[k * n + k] = -inv;
+        if (lane == 0) G[k * ld + k] = -inv;
     }
     __syncwarp();
     int i = 0, j = lane;
     tri_step(i, j, 0);
-    for (; i < n; tri_step(i, j, 32)) G[i * n + j] = -G[i * n + j];
+    for (; i < n; tri_step(i, j, 32)) G[i * ld + j] = -G[i * ld + j];
     __syncwarp();
     return true;
 }
@@ -158,15 +163,23 @@ __device__ inline void e_tridiag(cfloat* A, int n, int ld, const EighVec& V, int
         __syncwarp();
         // p = A22 u from the lower triangle, s = u^H p
         float s = 0.f;
+        // element (i, j) of the Hermitian A22 from the lower triangle
+        auto a22 = [&](int i, int j) {
+            cfloat x = j <= i ? A[i * ld + j] : A[j * ld + i];
+            if (j > i) x.im = -x.im;
+            return x;
+        };
         for (int i = k + 1 + lane; i < n; i += 32) {
             cfloat acc = A[i * ld + k + 1];  // u_{k+1} = 1
             if (i == k + 1) acc.im = 0.f;
-            for (int j = k + 2; j < n; ++j) {
-                const cfloat vj = A[j * ld + k];
-                cfloat aij = j <= i ? A[i * ld + j] : A[j * ld + i];
-                if (j > i) aij.im = -aij.im;
-                acc = cadd(acc, cmul(aij, vj));
+            cfloat acc2 = cmake(0.f, 0.f);  // two chains
+            int j = k + 2;
+            for (; j + 1 < n; j += 2) {
+                acc = cfma(acc, a22(i, j), A[j * ld + k]);
+                acc2 = cfma(acc2, a22(i, j + 1), A[(j + 1) * ld + k]);
             }
+            if (j < n) acc = cfma(acc, a22(i, j), A[j * ld + k]);
+            acc = cadd(acc, acc2);
             const cfloat vi = i == k + 1 ? cmake(1.f, 0.f) : A[i * ld + k];
             s += vi.re * acc.re + vi.im * acc.im;
             V.pw[i] = acc;
@@ -183,6 +196,7 @@ __device__ inline void e_tridiag(cfloat* A, int n, int ld, const EighVec& V, int
         const int m = n - k - 1, o = k + 1;
         int i = 0, j = lane;
         tri_step(i, j, 0);
+#pragma unroll 2
         for (; i < m; tri_step(i, j, 32)) {
             const cfloat wi = V.pw[o + i], wj = V.pw[o + j];
             const cfloat vi = i == 0 ? cmake(1.f, 0.f) : A[(o + i) * ld + k];

@@ -266,7 +266,8 @@ __global__ void __launch_bounds__(32) k_eigh(PixArgs a, EighLayout L) {
     const int lane = threadIdx.x;
     cfloat* C = reinterpret_cast<cfloat*>(eigh_smem + L.off_C);
     cfloat* A = reinterpret_cast<cfloat*>(eigh_smem + L.off_A);
-    double* G = reinterpret_cast<double*>(eigh_smem + L.off_G);
+    double* G = reinterpret_cast<double*>(eigh_smem + L.off_A);  // |Gamma| work matrix, until A is formed
+    double* col = reinterpret_cast<double*>(eigh_smem + L.off_col);
     const EighVec V = eigh_vectors(eigh_smem, L);
     cfloat* w = V.w;
     const int n = a.n, ld = L.ld, lag = a.baseline_lag;
@@ -284,16 +285,19 @@ __global__ void __launch_bounds__(32) k_eigh(PixArgs a, EighLayout L) {
                 const float f = rv[i] * rv[i];
                 C[i * ld + i] = cmake(f < 1e6f ? src[i] * f : 0.f, 0.f);
             }
-            for (int r = 1; r < n; ++r) {
-                const int o = r * (r - 1) / 2;
-                for (int c = lane; c < r; c += 32) {
-                    const float f = rv[r] * rv[c];
-                    cfloat v = f < 1e6f ? cmake(src[n + 2 * (o + c)] * f, src[n + 2 * (o + c) + 1] * f)
-                                        : cmake(0.f, 0.f);
-                    if (lag > 0 && r - c >= lag) v = cmake(0.f, 0.f);
-                    C[r * ld + c] = v;
-                    C[c * ld + r] = cconj(v);
-                }
+            // lower pairs (r, c), c < r, at e = r(r-1)/2 + c: every lane walks the pairs
+            // e = lane, lane + 32, ..., so its loads do not wait on one another
+            const int npairs = n * (n - 1) / 2;
+            int r = 1, c = lane;
+            while (c >= r) c -= r++;
+            for (int e = lane; e < npairs; e += 32) {
+                const float f = rv[r] * rv[c];
+                cfloat v = f < 1e6f ? cmake(src[n + 2 * e] * f, src[n + 2 * e + 1] * f) : cmake(0.f, 0.f);
+                if (lag > 0 && r - c >= lag) v = cmake(0.f, 0.f);
+                C[r * ld + c] = v;
+                C[c * ld + r] = cconj(v);
+                c += 32;
+                while (c >= r) c -= r++;
             }
         } else {
             const cfloat* src = a.Cin + p * n * n;
@@ -312,11 +316,14 @@ __global__ void __launch_bounds__(32) k_eigh(PixArgs a, EighLayout L) {
             // |Gamma| + 1e-6 I inverted in double; A = |Gamma|^{-1} o C (lower triangles)
             for (int i = 0; i < n; ++i)
                 for (int j = lane; j <= i; j += 32)
-                    G[i * n + j] = (double)s_gamma(a, C[i * ld + j], i == j) + (i == j ? 1e-6 : 0.0);
-            ok = e_inverse_spd(G, G + n * n, n, lane);
-            if (ok)
+                    G[i * ld + j] = (double)s_gamma(a, C[i * ld + j], i == j) + (i == j ? 1e-6 : 0.0);
+            ok = e_inverse_spd(G, ld, col, col + kEighMaxN, n, lane);
+            if (ok)  // in place: each element of G is read, then A written over it, by one lane
                 for (int i = 0; i < n; ++i)
-                    for (int j = lane; j <= i; j += 32) A[i * ld + j] = cscale(C[i * ld + j], (float)G[i * n + j]);
+                    for (int j = lane; j <= i; j += 32) {
+                        const float gi = (float)G[i * ld + j];
+                        A[i * ld + j] = cscale(C[i * ld + j], gi);
+                    }
         } else {
             for (int i = 0; i < n; ++i)
                 for (int j = lane; j <= i; j += 32) {

@@ -59,19 +59,37 @@ def test_fp64_precision_case():
     # SIMT form (fused, the coherence never stored) keeps the last iterate: it is compared
     # with the FP64 form doing the same.
     last = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form="fp64", eigh_fallback=False)
+    # the eigenvector's own conditioning, |A| / gap (A = |Gamma|^{-1} o C in float64, the
+    # gap to the eigenvalue next to the one nearest the 0.99 shift)
+    C64 = O.estimate_stack_covariance(z, hw, neighbor_arrays=nb, dtype=np.float64)
+    G = np.abs(C64) + 1e-6 * np.eye(cfg.nslc)
+    with np.errstate(all="ignore"):
+        w = np.linalg.eigvalsh(np.linalg.inv(G) * C64)
+    k = np.argmin(np.abs(w - 0.99), axis=-1)[..., None]
+    d = np.abs(w - np.take_along_axis(w, k, -1))
+    d.sort(axis=-1)
+    cond = np.abs(w).max(-1) / d[..., 1]
+    # relative rounding of each form's covariance sums: bf16 hi/lo products (about
+    # 2^-17), fp32 SIMT sums (a few ulp)
+    eps = {"tensor": 2.0 ** -17, "simt": 2.0 ** -22}
     for form, ref_form in (("tensor", out), ("simt", last)):
         f32 = np.zeros(z.shape[1:], np.uint8)
         o32 = dp.run_phase_linking(z, hw, neighbor_arrays=nb, covariance_form=form, nonconverged=f32)
         good = (ref_form.temp_coh > 0.3) & (diag["gamma_min_eig"] >= 1e-3)
         err = phase_err(o32.cpx_phase[:, good], ref_form.cpx_phase[:, good]).max(0)
+        tol = np.maximum(2e-3, eps[form] * cond[good])
         above = err > 1e-3
         differ = (f32.astype(bool) != flags.astype(bool))[good]
+        worst = int(np.argmax(err / tol))
         print(f"[fp64] form={form:6s} vs GPU float64: phase err max {err.max():.2e} rad on {good.sum()} pixels, "
               f"{int(above.sum())} above 1e-3 ({int((above & differ).sum())} of them where only one of the two "
-              f"forms met the stopping rule); {int(f32.sum())} / {int(flags.sum())} dense-eigensolver pixels")
+              f"forms met the stopping rule); {int(f32.sum())} / {int(flags.sum())} dense-eigensolver pixels; "
+              f"worst against its bound: {err[worst]:.2e} rad, |A|/gap {cond[good][worst]:.2e}")
         # slowly converging pixels (contraction near 1 per step) carry the stopping rule's
-        # own error, |step| / (1 - ratio), up to ~1e-3 rad in either form
-        assert err.max() < 2e-3 and above.mean() <= 1e-3
+        # own error, |step| / (1 - ratio), up to ~1e-3 rad in either form; where the
+        # eigenvalue gap is small the covariance's rounding moves the eigenvector by about
+        # eps |A| / gap, whatever solves it
+        assert np.all(err <= tol) and above.mean() <= 1e-3
 
 
 @pytest.mark.parametrize("kw", [
