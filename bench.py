@@ -530,8 +530,12 @@ def run_ours(args, rank, world, pool, cores):
         cv, cd = cpu_sample(pool, cores)
         cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": cd + " (numpy restatement of the reference algorithm)"}
-    # per block: k_ps_block, k_glrt_scale, k_glrt, k_prep, k_cov_tc, k_solve_reg, k_pixel (LU list), k_post
-    launches_per_step = len(plan) * 8
+    # per block: k_ps_block, k_glrt_scale, k_glrt, k_prep, k_cov_tc, k_solve_reg, k_pixel (LU list),
+    # k_eigh (pixels that missed the stopping rule), k_post
+    launches_per_step = len(plan) * 9
+    b_pl = 8 * NSLC + 8 + 2 + 8 * NSLC + 4 + 2 + 4 + 1 + 4 * NSLC + 4 * (NSLC - 2)
+    hbm_peak = float(peaks.get("hbm_gbs", 6768.8))
+    e2e_rate = px / (e2e_ms / 1000.0)
     line = {
         "metric": METRIC,
         "value": value,
@@ -568,6 +572,14 @@ def run_ours(args, rank, world, pool, cores):
                                 "note": "algorithmic covariance flops 4*W*N*(N+1) per pixel; peak = measured bf16 "
                                         "dense (of measured)"},
         "accuracy_vs_fp64": accuracy,
+        # algorithmic bytes per output pixel, B_PL: the stack 8N, mean and variance 8, PS and
+        # nodata masks 2, cpx_phase 8N, temp_coh 4, shp_counts 2, eigenvalue 4, estimator 1,
+        # CRLB 4N, closure phases 4(N - 2); the PS pass adds 8N + 9
+        "achieved_gbs": {"b_pl_bytes_per_pixel": b_pl, "ps_pass_bytes_per_pixel": 8 * NSLC + 9,
+                         "value": (b_pl + 8 * NSLC + 9) * value / 1e9,
+                         "e2e": (b_pl + 8 * NSLC + 9) * e2e_rate / 1e9, "unit": "GB/s",
+                         "hbm_peak": hbm_peak,
+                         "note": "B_PL x pixels/s: far below HBM (the path is compute-bound); of measured"},
         "clocks": clocks,
         "forms": {"blocks": len(sub), "unit": UNIT, "chosen": chosen_rate, "plain": plain_rate,
                   "chosen_over_plain": chosen_rate / plain_rate, "evd_chosen": evd_rate,
