@@ -38,6 +38,7 @@ from .shp import estimate_neighbors
 from .similarity import get_circle_idxs, max_similarity, median_similarity, stack_similarity
 from .workflow import (
     StridedBlockManager,
+    clear_loop_graphs,
     grow_nodata_region,
     plan_ministacks,
     run_wrapped_phase_sequential,
@@ -54,6 +55,7 @@ __all__ = [
     "Strides",
     "StridedBlockManager",
     "calc_ps_block",
+    "clear_loop_graphs",
     "compress",
     "deferred_checks",
     "estimate_neighbors",

@@ -85,6 +85,31 @@ def deferred_checks():
         _lib.check(lib.dpl_phase_link_status_words(nslc, words.data_ptr()), "dpl_phase_link")
 
 
+@contextlib.contextmanager
+def _captured_checks(calls):
+    """Inside the block (a CUDA-graph capture of device-resident calls), each
+    ``run_phase_linking`` call enqueues its pipeline without a host copy or event and
+    appends ``(params, workspace)`` to ``calls``; after a replay, ``check_captured``
+    reports the first failure in call order."""
+    prev = getattr(_deferred, "pending", None)
+    prev_graph = getattr(_deferred, "graph", None)
+    _deferred.pending = []
+    _deferred.graph = calls
+    try:
+        yield calls
+    finally:
+        _deferred.pending = prev
+        _deferred.graph = prev_graph
+
+
+def check_captured(calls):
+    """Status of the captured calls after a replay (synchronises the stream), raising
+    the exception the first failing synchronous call would have raised."""
+    lib = _lib.load()
+    for prm, ws in calls:
+        _lib.check(lib.dpl_phase_link_status(prm, D.ptr(ws), ws.numel(), D.stream_handle()), "dpl_phase_link")
+
+
 def _is_complex(x) -> bool:
     if D.is_device_tensor(x):
         return x.is_complex()
@@ -207,7 +232,12 @@ def run_phase_linking(
                           eigenvalues=D.ptr(eig), estimator=D.ptr(est), crlb_std_dev=D.ptr(crlb),
                           closure_phases=D.ptr(clos) if nslc > 2 else None, nonconverged=D.ptr(ncflag))
     pending = getattr(_deferred, "pending", None) if on_device else None
-    if pending is None:
+    captured = getattr(_deferred, "graph", None) if on_device else None
+    if captured is not None:
+        _lib.check(lib.dpl_phase_link_async(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle()),
+                   "dpl_phase_link_async")
+        captured.append((prm, ws))
+    elif pending is None:
         st = lib.dpl_phase_link(prm, inp, outp, D.ptr(ws), ws.numel(), D.stream_handle())
         _lib.check(st, "dpl_phase_link")
     else:

@@ -43,7 +43,7 @@ from . import _device as D
 from . import _lib
 from ._types import HalfWindow, ShpMethod, Strides
 from .compress import compress
-from .phase_link import deferred_checks, run_phase_linking
+from .phase_link import _captured_checks, check_captured, deferred_checks, run_phase_linking
 from .ps import calc_ps_block
 from .shp import estimate_neighbors
 from .similarity import stack_similarity
@@ -59,6 +59,7 @@ __all__ = [
     "iter_blocks",
     "plan_ministacks",
     "run_wrapped_phase_sequential",
+    "clear_loop_graphs",
     "run_wrapped_phase_single",
 ]
 
@@ -324,12 +325,19 @@ def run_wrapped_phase_single(slc_stack, *, half_window, strides=None, first_real
                              shp_nslc: Optional[int] = None, similarity_nearest_n: Optional[int] = None,
                              write_closure_phase: bool = True, write_crlb: bool = True,
                              block_shape=(512, 512), baseline_lag: Optional[int] = None,
-                             similarity: bool = True) -> SingleOutput:
+                             similarity: bool = True, graph: bool = False) -> SingleOutput:
     """One ministack's block loop on a (n, R, C) complex stack (CUDA tensor or host
     array; the results are CUDA tensors).  ``half_window`` and ``strides`` are
     ``{"y": .., "x": ..}`` dicts or (y, x) pairs; ``amp_mean`` / ``amp_dispersion`` are
     the (R, C) rasters the reference reads from files (variance = (dispersion *
-    mean) ** 2)."""
+    mean) ** 2).
+
+    ``graph`` (not in the reference): the whole block loop, similarity included, runs as
+    one CUDA graph.  The first call with a given set of shapes, parameters and skipped
+    blocks runs eagerly on the graph's own input buffers and captures the loop; later
+    such calls copy their inputs into those buffers and replay it (one launch from the
+    host), then check every block's phase-linking status in order.  The results are
+    copies, the same as the eager loop's.  KS SHPs run eagerly."""
     torch = D.require_cuda()
     hw = _yx(half_window, HalfWindow)
     st = _yx(strides if strides is not None else (1, 1), Strides)
@@ -374,19 +382,68 @@ def run_wrapped_phase_single(slc_stack, *, half_window, strides=None, first_real
         checks.append(torch.stack([nodata[ir, ic].all(), (cur == 0).all() | nan.all(),
                                    nan.flatten(1).all(dim=1).any()]))
     skip = torch.stack(checks).any(dim=1).tolist() if checks else []
-    with deferred_checks():
+
+    def loop(inp, rasters):
+        # the blocks, the similarity and the uint16 shp_counts raster
+        z, nd, ps_, mn, vr = inp
         for (out_b, trim, in_b, no_pad, in_trim), skipped in zip(blocks, skip):
             if not skipped:
-                _single_block(stack, out_b, trim, in_b, no_pad, in_trim, nodata, psm, mean, var, hw, st, method,
-                              shp_alpha, shp_nslc, use_evd, beta, zero_correlation_threshold, output_reference_idx,
-                              baseline_lag, first_real_slc_idx, write_crlb, compressed_reference_idx,
-                              (pl, crlb, clos, comp, disp, tcoh, counts, eig, est))
+                _single_block(z, out_b, trim, in_b, no_pad, in_trim, nd, ps_, mn, vr, hw, st, method, shp_alpha,
+                              shp_nslc, use_evd, beta, zero_correlation_threshold, output_reference_idx,
+                              baseline_lag, first_real_slc_idx, write_crlb, compressed_reference_idx, rasters)
+        pl_, crlb_, clos_, comp_, disp_, tcoh_, counts_, eig_, est_ = rasters
+        sim = None
+        if similarity:
+            sim = stack_similarity(pl_, search_radius=7, sim_type="median", nearest_n=similarity_nearest_n)
+        return SingleOutput(pl_, crlb_, clos_, comp_, disp_, tcoh_, counts_.clamp(0, 65535).to(torch.uint16), eig_,
+                            est_, sim)
 
-    sim = None
-    if similarity:
-        sim = stack_similarity(pl, search_radius=7, sim_type="median", nearest_n=similarity_nearest_n)
-    # the shp_counts raster is uint16
-    return SingleOutput(pl, crlb, clos, comp, disp, tcoh, counts.clamp(0, 65535).to(torch.uint16), eig, est, sim)
+    rasters = (pl, crlb, clos, comp, disp, tcoh, counts, eig, est)
+    inputs = (stack, nodata, psm, mean, var)
+    # the KS test copies a host table per call, which a graph cannot replay: eager
+    if not graph or method == ShpMethod.KS:
+        with deferred_checks():
+            return loop(inputs, rasters)
+    key = (str(dev), n, rows, cols, hw, st, first_real_slc_idx, output_reference_idx, compressed_reference_idx,
+           float(beta), float(zero_correlation_threshold), bool(use_evd), method, float(shp_alpha), shp_nslc,
+           similarity_nearest_n, bool(write_closure_phase), bool(write_crlb), tuple(block_shape), baseline_lag,
+           bool(similarity), mean is None, var is None, tuple(skip))
+    entry = _LOOP_GRAPHS.get(key)
+    if entry is None:
+        # eager run on the graph's own input buffers (it also sets up every kernel),
+        # then the capture of the same loop on a side stream
+        static_in = tuple(None if x is None else x.clone() for x in inputs)
+        with deferred_checks():
+            out = loop(static_in, rasters)
+        calls = []
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(side), torch.cuda.graph(g, stream=side), _captured_checks(calls):
+            captured = loop(static_in, rasters)
+        torch.cuda.current_stream().wait_stream(side)
+        while len(_LOOP_GRAPHS) >= _LOOP_GRAPHS_MAX:
+            _LOOP_GRAPHS.pop(next(iter(_LOOP_GRAPHS)))
+        _LOOP_GRAPHS[key] = (static_in, g, calls, captured)
+    else:
+        static_in, g, calls, out = entry
+        for dst, src in zip(static_in, inputs):
+            if dst is not None:
+                dst.copy_(src)
+        g.replay()
+        check_captured(calls)
+    return SingleOutput(*(None if x is None else x.clone() for x in out))
+
+
+# Captured block loops (run_wrapped_phase_single(graph=True)), oldest first: the input
+# buffers, the graph, its phase-linking calls (params, workspace) and its outputs.
+_LOOP_GRAPHS: dict = {}
+_LOOP_GRAPHS_MAX = 4
+
+
+def clear_loop_graphs():
+    """Drop the captured block loops and the device memory they hold."""
+    _LOOP_GRAPHS.clear()
 
 
 def _single_block(stack, out_b, trim, in_b, no_pad, in_trim, nodata, psm, mean, var, hw, st, method, shp_alpha,
@@ -468,10 +525,12 @@ def run_wrapped_phase_sequential(slc_stack, *, ministack_size: int, half_window,
                                  compressed_slc_plan: CompressedSlcPlan | str = CompressedSlcPlan.ALWAYS_FIRST,
                                  max_num_compressed: int = 100, output_reference_idx: Optional[int] = None,
                                  new_compressed_reference_idx: Optional[int] = None, write_closure_phase: bool = True,
-                                 write_crlb: bool = True, block_shape=(512, 512), baseline_lag: Optional[int] = None
-                                 ) -> SequentialOutput:
+                                 write_crlb: bool = True, block_shape=(512, 512), baseline_lag: Optional[int] = None,
+                                 graph: bool = False) -> SequentialOutput:
     """The sequential estimator on a (n, R, C) complex stack: ministacks of
-    ``ministack_size`` real SLCs, each led by the compressed SLCs of the ones before."""
+    ``ministack_size`` real SLCs, each led by the compressed SLCs of the ones before.
+    ``graph``: each ministack's block loop as one CUDA graph (see
+    ``run_wrapped_phase_single``)."""
     torch = D.require_cuda()
     stack = D.to_device(slc_stack, np.complex64)
     n = int(stack.shape[0])
@@ -494,7 +553,7 @@ def run_wrapped_phase_sequential(slc_stack, *, ministack_size: int, half_window,
             nodata_mask=nodata_mask, ps_mask=ps_mask, amp_mean=amp_mean, amp_dispersion=amp_dispersion,
             shp_method=shp_method, shp_alpha=shp_alpha, shp_nslc=shp_nslc, similarity_nearest_n=similarity_nearest_n,
             write_closure_phase=write_closure_phase, write_crlb=write_crlb, block_shape=block_shape,
-            baseline_lag=baseline_lag)
+            baseline_lag=baseline_lag, graph=graph)
         comp_list.append(res.comp_slc)
         pls.append(res.pl_slcs)
         crlbs.append(res.crlb)

@@ -209,3 +209,49 @@ def test_block_with_an_all_nan_slc_is_skipped():
     assert (_np(res.pl_slcs)[:, 25:35, 1:13] == 0).all()
     assert (tc[25:35, 16:22] > 0).all()
     assert (tc[16:22, 16:22] > 0).all()
+
+
+def test_block_loop_as_one_graph_matches_eager():
+    """graph=True: the first call captures the block loop (similarity included); a second
+    call with new data of the same shapes replays it.  Both must equal the eager loop on
+    the same data, a skipped block (all-zero input) included."""
+    from dolphin_gb300.workflow import clear_loop_graphs
+
+    clear_loop_graphs()
+    kw = dict(half_window=(2, 3), strides=(1, 2), block_shape=(20, 24), shp_method="glrt", shp_alpha=0.05)
+    for seed in (906, 907):
+        cfg = StackConfig(nslc=8, rows=52, cols=60, seed=seed, ps_frac=0.03)
+        z = make_stack(cfg)
+        z[:, :30, :40] = 0  # covers the first block's padded input: skipped in both runs
+        amp = np.abs(z)
+        mean = amp.mean(0).astype(np.float32)
+        disp = (amp.std(0) / np.maximum(mean, 1e-6)).astype(np.float32)
+        ps = disp < 0.25
+        zd = torch.from_numpy(z).cuda()
+        args = dict(kw, ps_mask=ps, amp_mean=mean, amp_dispersion=disp)
+        eager = _single_dict(W.run_wrapped_phase_single(zd, **args))
+        graphed = _single_dict(W.run_wrapped_phase_single(zd, graph=True, **args))
+        for k in KEYS:
+            np.testing.assert_array_equal(graphed[k], eager[k], err_msg=k)
+        assert (eager["tc"] == 0).any()  # a skipped block keeps its zeros
+    clear_loop_graphs()
+
+
+def test_sequential_as_graphs_matches_eager():
+    cfg = StackConfig(nslc=10, rows=40, cols=44, seed=908, ps_frac=0.03)
+    z = make_stack(cfg)
+    zd = torch.from_numpy(z).cuda()
+    amp = np.abs(z)
+    mean = amp.mean(0).astype(np.float32)
+    disp = (amp.std(0) / np.maximum(mean, 1e-6)).astype(np.float32)
+    kw = dict(ministack_size=5, half_window=(2, 2), block_shape=(20, 24), shp_method="glrt", amp_mean=mean,
+              amp_dispersion=disp, ps_mask=disp < 0.25)
+    eager = W.run_wrapped_phase_sequential(zd, **kw)
+    for _rep in range(2):  # capture, then replay
+        graphed = W.run_wrapped_phase_sequential(zd, graph=True, **kw)
+        np.testing.assert_array_equal(_np(graphed.pl_slcs), _np(eager.pl_slcs))
+        for a, b in zip(graphed.temp_coh, eager.temp_coh):
+            np.testing.assert_array_equal(_np(a), _np(b))
+        for a, b in zip(graphed.comp_slcs, eager.comp_slcs):
+            np.testing.assert_array_equal(_np(a), _np(b))
+    W.clear_loop_graphs()
