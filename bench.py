@@ -791,11 +791,12 @@ def run_parity(args):
         blk, mean, disp, ps, nb = block_inputs(dp, stack, entry)
         (t0, t1), (c0, c1) = entry[2], entry[3]
         kw = dict(ps_mask=ps, neighbor_arrays=nb, avg_mag=mean, compute_crlb=True)
-        outs = {}
+        outs, ncf = {}, {}
         for form in ("fp64", "tensor", "simt"):
+            ncf[form] = torch.zeros(blk.shape[1:], dtype=torch.uint8, device=blk.device)
             torch.cuda.synchronize()
             w0 = time.perf_counter()
-            outs[form] = dp.run_phase_linking(blk, HALF, covariance_form=form, **kw)
+            outs[form] = dp.run_phase_linking(blk, HALF, covariance_form=form, nonconverged=ncf[form], **kw)
             torch.cuda.synchronize()
             secs[form] += time.perf_counter() - w0
         trim = (slice(t0, t1), slice(c0, c1))
@@ -819,6 +820,13 @@ def run_parity(args):
             a["flips_fp64_emi"] += int((flip & (ref.estimator[trim] == 1)).sum())
             if (flip & good).any():
                 a["flips_phase_max_rad"] = max(a["flips_phase_max_rad"], float(d[flip & good].max()))
+            # the pixels above 1e-3 rad, in frame coordinates, with both forms' flags for
+            # the dense eigensolver (set where the iteration missed its stopping rule)
+            for r, c in (good & (d > 1e-3)).nonzero().tolist()[:20]:
+                a.setdefault("above_1e-3_pixels", []).append({
+                    "row": entry[4][0] + r, "col": entry[5][0] + c, "rad": float(d[r, c]),
+                    "fp64_temp_coh": float(ref.temp_coh[trim][r, c]),
+                    "nonconverged": int(ncf[form][trim][r, c]), "fp64_nonconverged": int(ncf["fp64"][trim][r, c])})
         tests, near, differ = glrt_check(torch, mean, disp, nb, NSLC, ALPHA)
         glrt["tests"] += tests
         glrt["near_cutoff_1e-6"] += near
